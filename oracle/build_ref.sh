@@ -1,0 +1,30 @@
+#!/bin/bash
+# Builds the UNMODIFIED CAPS reference (one rank) from its own sources into
+# oracle/_ref/, for cross-checking the oracle restatement.  Runs only where the
+# reference sources are present; outputs never leave oracle/_ref/ (git-ignored).
+#   oracle/_ref/fromfile1, oracle/_ref/randombenchmark   the reference drivers
+#   oracle/_ref/libcapsref.so                           multiply() & friends
+# Usage: oracle/build_ref.sh [REFERENCE_DIR] [THREADS]
+set -euo pipefail
+here="$(cd "$(dirname "$0")" && pwd)"
+ref="${1:-/root/reference}"
+threads="${2:-$(nproc)}"
+out="$here/_ref"
+[ -f "$ref/multiply.cpp" ] || { echo "reference sources not found at $ref" >&2; exit 3; }
+blasdir="$(python3 -c 'import numpy,os; print(os.path.realpath(os.path.join(os.path.dirname(numpy.__file__), os.pardir, "numpy.libs")))')"
+blaslib="$(ls "$blasdir"/libscipy_openblas64_*.so | head -1)"
+mkdir -p "$out"
+CXX="g++ -O3 -fopenmp -DNUM_THREADS=$threads -include $here/ref_shim/mpi.h -I$here/ref_shim -I$ref -w"
+srcs="communication.cpp matrix.cpp multiply.cpp memory.cpp dgemm-blas.cpp counters.cpp library.cpp summa1d.cpp"
+objs=""
+for s in $srcs; do
+  $CXX -fPIC -c "$ref/$s" -o "$out/${s%.cpp}.o"
+  objs="$objs $out/${s%.cpp}.o"
+done
+gcc -O2 -fPIC -c "$here/ref_shim/blas_lp64.c" -o "$out/blas_lp64.o"
+link="$out/blas_lp64.o $blaslib -Wl,-rpath,$blasdir"
+$CXX -shared -o "$out/libcapsref.so" $objs $link
+$CXX "$ref/fromfile1.cpp" $objs $link -o "$out/fromfile1"
+$CXX "$ref/randombenchmark.cpp" $objs $link -o "$out/randombenchmark"
+rm -f "$out"/*.o
+echo "built $out (threads=$threads, blas=$blaslib)"

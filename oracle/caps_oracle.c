@@ -1,0 +1,420 @@
+/*
+ * caps_oracle.c -- CPU oracle for the CAPS Strassen multiply path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker that the CUDA path is
+ * compared against (tests, smoke check) and the timed CPU restatement of the
+ * reference's own CPU path (the "port" baseline in bench.py).  Nothing in the
+ * product library links, loads or calls it.
+ *
+ * Parity pins: the integer known-answer fixtures of the reference
+ * (tests/test{28,42,56,196,294,392}.{in,correct}) and, in the build container,
+ * bit-for-bit agreement with the reference's own multiply() compiled unmodified
+ * (oracle/build_ref.sh) on random float inputs with the same BLAS.
+ *
+ * What it restates (file:line in the CAPS sources):
+ *   - recursive block layout and its reorder:   communication.cpp:612-704,
+ *                                               matrix.h:20-44, matrix.cpp:9-12
+ *   - Strassen-Winograd step ('d' and 'b'):     multiply.cpp:409-454 (DFS, OpenMP
+ *     variant) and multiply.cpp:212-310 (BFS; per-element identical arithmetic)
+ *   - element-wise additions / C combination:   multiply.cpp:110-210
+ *   - base case with bs repack:                 multiply.cpp:1082-1141,
+ *                                               dgemm-blas.cpp:4-13
+ *   - pattern dispatch on one rank:             multiply.cpp:28-108
+ * plus a double-double classical product (Ogita, Rump, Oishi 2005, "Accurate
+ * sum and dot product", algorithm Dot2) used as the float oracle, and a CPU
+ * model of the split-integer base case that the GPU form must match exactly.
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef void (*dgemm_ilp64_fn)(const char *, const char *, const int64_t *,
+                               const int64_t *, const int64_t *, const double *,
+                               const double *, const int64_t *, const double *,
+                               const int64_t *, const double *, double *,
+                               const int64_t *);
+
+static dgemm_ilp64_fn g_dgemm = 0;     /* optional BLAS (ILP64 Fortran ABI) */
+static int g_threads = 1;
+
+/* Installs an ILP64 Fortran dgemm (e.g. OpenBLAS's scipy_dgemm_64_) as the
+ * base-case multiply; NULL restores the built-in classical loop. */
+void caps_oracle_set_dgemm(void *fn) { g_dgemm = (dgemm_ilp64_fn)fn; }
+void caps_oracle_set_threads(int t) { g_threads = t > 0 ? t : 1; }
+
+/* ---------------------------------------------------------------------- */
+/* Layout: index of element (r, c) of an n x n matrix in CAPS block layout  */
+/* with nrec recursive levels (quadrant order 11, 21, 12, 22) and bs x bs   */
+/* column-major blocks, blocks column-major within the leaf.                */
+/* communication.cpp:612-655 (distribute), :661-704 (collect), 1 rank.      */
+/* ---------------------------------------------------------------------- */
+int64_t caps_oracle_layout_index(int64_t n, int nrec, int64_t bs, int64_t r, int64_t c)
+{
+    int64_t off = 0, size = n;
+    for (int l = 0; l < nrec; l++) {
+        int64_t h = size / 2;
+        int64_t q = (r >= h ? 1 : 0) + (c >= h ? 2 : 0);
+        off += q * h * h;
+        if (r >= h) r -= h;
+        if (c >= h) c -= h;
+        size = h;
+    }
+    int64_t nb = size / bs;
+    off += ((r / bs) + (c / bs) * nb) * bs * bs + (c % bs) * bs + (r % bs);
+    return off;
+}
+
+/* column-major n x n (ld = n)  ->  CAPS layout.   distributeFrom1Proc. */
+void caps_oracle_to_caps(int64_t n, int nrec, int64_t bs, const double *colmajor, double *caps)
+{
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t c = 0; c < n; c++)
+        for (int64_t r = 0; r < n; r++)
+            caps[caps_oracle_layout_index(n, nrec, bs, r, c)] = colmajor[r + c * n];
+}
+
+/* CAPS layout -> column-major.   collectTo1Proc. */
+void caps_oracle_from_caps(int64_t n, int nrec, int64_t bs, const double *caps, double *colmajor)
+{
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t c = 0; c < n; c++)
+        for (int64_t r = 0; r < n; r++)
+            colmajor[r + c * n] = caps[caps_oracle_layout_index(n, nrec, bs, r, c)];
+}
+
+/* ---------------------------------------------------------------------- */
+/* Base case: C = A * B for an m x m leaf (multiply.cpp:1082-1141).        */
+/* ---------------------------------------------------------------------- */
+static void classical_colmajor(int64_t m, const double *A, const double *B, double *C)
+{
+    /* C(:,j) = sum_k A(:,k) * B(k,j): one rounding per multiply and add,
+     * k ascending, like a reference (unblocked) Fortran dgemm. */
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t j = 0; j < m; j++) {
+        double *cj = C + j * m;
+        for (int64_t i = 0; i < m; i++) cj[i] = 0.0;
+        for (int64_t k = 0; k < m; k++) {
+            double b = B[k + j * m];
+            const double *ak = A + k * m;
+            for (int64_t i = 0; i < m; i++) cj[i] += ak[i] * b;
+        }
+    }
+}
+
+static void leaf_dgemm(int64_t m, const double *A, const double *B, double *C)
+{
+    if (g_dgemm) {
+        const char N = 'N';
+        const double one = 1.0, zero = 0.0;
+        int64_t mm = m;
+        g_dgemm(&N, &N, &mm, &mm, &mm, &one, A, &mm, B, &mm, &zero, C, &mm);
+    } else {
+        classical_colmajor(m, A, B, C);
+    }
+}
+
+/* block_multiply: repack bs-blocked leaf into column-major when 1<bs<m. */
+static void base_case(int64_t m, int64_t bs, const double *A, const double *B, double *C)
+{
+    if (bs == 1 || bs == m) {
+        leaf_dgemm(m, A, B, C);
+        return;
+    }
+    int64_t nb = m / bs, mm = m * m;
+    double *w = (double *)malloc((size_t)(3 * mm) * sizeof(double));
+    double *AA = w, *BB = w + mm, *CC = w + 2 * mm;
+    for (int64_t col = 0; col < m; col++) {
+        int64_t cb = col / bs, cr = col % bs;
+        for (int64_t rb = 0; rb < nb; rb++) {
+            memcpy(AA + col * m + rb * bs, A + (rb + cb * nb) * bs * bs + cr * bs, (size_t)bs * sizeof(double));
+            memcpy(BB + col * m + rb * bs, B + (rb + cb * nb) * bs * bs + cr * bs, (size_t)bs * sizeof(double));
+        }
+    }
+    leaf_dgemm(m, AA, BB, CC);
+    for (int64_t col = 0; col < m; col++) {
+        int64_t cb = col / bs, cr = col % bs;
+        for (int64_t rb = 0; rb < nb; rb++)
+            memcpy(C + (rb + cb * nb) * bs * bs + cr * bs, CC + col * m + rb * bs, (size_t)bs * sizeof(double));
+    }
+    free(w);
+}
+
+/* ---------------------------------------------------------------------- */
+/* One Strassen-Winograd step on CAPS layout, multiply.cpp:409-454.        */
+/* Quadrant offsets 0,1,2,3 x q for X11, X21, X12, X22 (multiply.cpp:334). */
+/* ---------------------------------------------------------------------- */
+static int64_t g_adds = 0, g_muls = 0;
+
+static void rec(const double *A, const double *B, double *C, int64_t n, int nrec, int64_t bs,
+                const char *pattern);
+
+static void step(const double *A, const double *B, double *C, int64_t n, int nrec, int64_t bs,
+                 const char *pattern)
+{
+    int64_t h = n / 2, q = h * h;
+    const double *A11 = A, *A21 = A + q, *A12 = A + 2 * q, *A22 = A + 3 * q;
+    const double *B11 = B, *B21 = B + q, *B12 = B + 2 * q, *B22 = B + 3 * q;
+    double *C11 = C, *C21 = C + q, *C12 = C + 2 * q, *C22 = C + 3 * q;
+    double *W = (double *)malloc((size_t)(9 * q) * sizeof(double));
+    double *T3 = W, *T4 = W + q, *T5 = W + 2 * q, *T6 = W + 3 * q;
+    double *S3 = W + 4 * q, *S4 = W + 5 * q, *S5 = W + 6 * q, *S7 = W + 7 * q;
+    double *Qt = W + 8 * q;
+    /* S/T sums: same per-element formulas and order as the reference
+     * (tripleSubMatrices/addSubMatrices/subMatrices, :421-435). */
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t i = 0; i < q; i++) {
+        S5[i] = B22[i] - B12[i];
+        S3[i] = B12[i] - B11[i];
+        S4[i] = B22[i] - S3[i];
+        T3[i] = A21[i] + A22[i];
+        T5[i] = A11[i] - A21[i];
+        T4[i] = T3[i] - A11[i];
+        T6[i] = A12[i] - T4[i];
+        S7[i] = S4[i] - B21[i];
+    }
+    g_adds += 8 * q;
+    /* Q1 -> C11 (kept as Q1 until C11 = Q1 + Q2). The C combination
+     * (calcCij, :195-210 / :444-451):
+     *   C11 = Q1+Q2;  U1 = Q1+Q4;  U2 = U1+Q5;  C21 = U2-Q7;  C22 = U2+Q3;
+     *   U3 = U1+Q3;   C12 = U3+Q6. */
+    double *U = (double *)malloc((size_t)(2 * q) * sizeof(double));
+    double *U2 = U, *U3 = U + q;
+    rec(A11, B11, C11, h, nrec - 1, bs, pattern);          /* Q1 in C11 */
+    rec(T4, S4, Qt, h, nrec - 1, bs, pattern);              /* Q4 */
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t i = 0; i < q; i++) { double u1 = C11[i] + Qt[i]; U2[i] = u1; U3[i] = u1; }
+    rec(T5, S5, Qt, h, nrec - 1, bs, pattern);              /* Q5 */
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t i = 0; i < q; i++) U2[i] = U2[i] + Qt[i];
+    rec(T3, S3, Qt, h, nrec - 1, bs, pattern);              /* Q3 */
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t i = 0; i < q; i++) { C22[i] = U2[i] + Qt[i]; U3[i] = U3[i] + Qt[i]; }
+    rec(A22, S7, Qt, h, nrec - 1, bs, pattern);             /* Q7 */
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t i = 0; i < q; i++) C21[i] = U2[i] - Qt[i];
+    rec(T6, B22, Qt, h, nrec - 1, bs, pattern);             /* Q6 */
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t i = 0; i < q; i++) C12[i] = U3[i] + Qt[i];
+    rec(A12, B21, Qt, h, nrec - 1, bs, pattern);            /* Q2 */
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t i = 0; i < q; i++) C11[i] = C11[i] + Qt[i];
+    g_adds += 7 * q;
+    free(U);
+    free(W);
+}
+
+static int g_bad_pattern = 0;
+
+/* multiplyInternal on one rank (multiply.cpp:28-108): 'b','d','h' (and NULL)
+ * all perform the same per-element Winograd arithmetic on one process. */
+static void rec(const double *A, const double *B, double *C, int64_t n, int nrec, int64_t bs,
+                const char *pattern)
+{
+    if (nrec == 0) {
+        g_adds += n * n * n;
+        g_muls += n * n * n;
+        base_case(n, bs, A, B, C);
+        return;
+    }
+    if (pattern) {
+        char p = pattern[0];
+        if (!(p == 'b' || p == 'B' || p == 'd' || p == 'D' || p == 'h' || p == 'H')) {
+            g_bad_pattern = 1;
+            return;
+        }
+        pattern++;
+    }
+    step(A, B, C, n, nrec, bs, pattern);
+}
+
+/* multiply() on one rank (multiply.cpp:9-25).  Returns 0, or -1 for an
+ * invalid pattern character, -2 for a size the layout cannot hold. */
+int caps_oracle_multiply(const double *A, const double *B, double *C, int64_t n, int nrec,
+                         int64_t bs, const char *pattern)
+{
+    if (n <= 0 || nrec < 0 || bs <= 0 || (n % (((int64_t)1 << nrec) * bs)) != 0) return -2;
+    g_bad_pattern = 0;
+    rec(A, B, C, n, nrec, bs, pattern);
+    return g_bad_pattern ? -1 : 0;
+}
+
+/* add/multiply counters as the reference counts them (counters.cpp). */
+void caps_oracle_counters(int64_t *adds, int64_t *muls) { *adds = g_adds; *muls = g_muls; }
+void caps_oracle_reset_counters(void) { g_adds = 0; g_muls = 0; }
+
+/* ---------------------------------------------------------------------- */
+/* Double-double classical product (Dot2 of Ogita-Rump-Oishi):             */
+/* result as if accumulated in twice the working precision.  Column-major. */
+/* ---------------------------------------------------------------------- */
+static inline void two_sum(double a, double b, double *s, double *e)
+{
+    double x = a + b, z = x - a;
+    *s = x;
+    *e = (a - (x - z)) + (b - z);
+}
+
+static inline void dot2_acc(double a, double b, double *s, double *c)
+{
+    double p = a * b;
+    double pe = fma(a, b, -p);
+    double t, te;
+    two_sum(*s, p, &t, &te);
+    *s = t;
+    *c += te + pe;
+}
+
+/* hi/lo of sum_k A(i,k) B(k,j) for every (i, j); A, B column-major n x n. */
+void caps_oracle_dd_gemm(int64_t n, const double *A, const double *B, double *Chi, double *Clo)
+{
+    double *At = (double *)malloc((size_t)(n * n) * sizeof(double));
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t i = 0; i < n; i++)
+        for (int64_t k = 0; k < n; k++) At[k + i * n] = A[i + k * n];
+#pragma omp parallel for num_threads(g_threads) schedule(dynamic, 4)
+    for (int64_t j = 0; j < n; j++) {
+        const double *bj = B + j * n;
+        for (int64_t i = 0; i < n; i++) {
+            const double *ai = At + i * n;
+            double s = 0.0, c = 0.0;
+            for (int64_t k = 0; k < n; k++) dot2_acc(ai[k], bj[k], &s, &c);
+            double hi = s + c;
+            Chi[i + j * n] = hi;
+            Clo[i + j * n] = c - (hi - s);
+        }
+    }
+    free(At);
+}
+
+/* Sampled entries of the same product: rows[t], cols[t] for t < count. */
+void caps_oracle_dd_entries(int64_t n, const double *A, const double *B, const int64_t *rows,
+                            const int64_t *cols, int64_t count, double *hi, double *lo)
+{
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t t = 0; t < count; t++) {
+        int64_t i = rows[t], j = cols[t];
+        double s = 0.0, c = 0.0;
+        for (int64_t k = 0; k < n; k++) dot2_acc(A[i + k * n], B[k + j * n], &s, &c);
+        double h = s + c;
+        hi[t] = h;
+        lo[t] = c - (h - s);
+    }
+}
+
+/* |A||B| entries (classical, double), used to normalise element-wise error. */
+void caps_oracle_absprod_entries(int64_t n, const double *A, const double *B, const int64_t *rows,
+                                 const int64_t *cols, int64_t count, double *out)
+{
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t t = 0; t < count; t++) {
+        int64_t i = rows[t], j = cols[t];
+        double s = 0.0;
+        for (int64_t k = 0; k < n; k++) s += fabs(A[i + k * n]) * fabs(B[k + j * n]);
+        out[t] = s;
+    }
+}
+
+/* ---------------------------------------------------------------------- */
+/* CPU model of the split-integer base case (the GPU "split" form).        */
+/* Not a reference algorithm: the reference has only the FP64 dgemm.  It   */
+/* states the exact integer arithmetic the GPU kernel performs, so the two */
+/* must agree bit for bit.                                                 */
+/*                                                                         */
+/* Row i of A is scaled by 2^fa[i], column j of B by 2^fb[j], with         */
+/* fa = 55 - Ea (|a| < 2^Ea over the row), rounded to integers X (|X| <=    */
+/* 2^55) and cut into s balanced base-128 digits d_1..d_s (|d| <= 64),     */
+/* most significant first.  The product keeps the digit pairs (a, b) with  */
+/* a + b <= nd + 1; pair sums are exact integers.  Diagonals t = a + b are */
+/* combined as hi = sum_{t<=5} c_t 2^(7(5-t)), lo = sum_{t>=6} c_t         */
+/* 2^(7(9-t)), and the leaf value is (hi 2^28 + lo) 2^(7(s_ref)) 2^-(fa+fb) */
+/* rounded once.                                                           */
+/* ---------------------------------------------------------------------- */
+#define SPLIT_BETA 7
+
+/* exponent E with |x| < 2^E, read from the IEEE exponent field (subnormals
+ * count as 2^-1022); -100000 for zero.  Same rule as the GPU slicer. */
+static int exp_bound(double x)
+{
+    uint64_t u;
+    memcpy(&u, &x, 8);
+    int field = (int)((u >> 52) & 0x7ff);
+    if ((u & 0x7fffffffffffffffULL) == 0) return -100000;
+    if (field == 0) return -1022;
+    return field - 1022;
+}
+
+/* digits of round(x * 2^f) in balanced base 128, s digits, MS first. */
+static void split_digits(double x, int f, int s, int *d)
+{
+    /* X = round-half-even(x 2^f) as int64; |X| <= 2^55 by construction */
+    double y = ldexp(x, f);
+    int64_t X = (int64_t)nearbyint(y);
+    /* least significant digit first */
+    int64_t R = X;
+    int tmp[16];
+    int total = 8; /* 8 digits cover 56 bits */
+    for (int k = 0; k < total; k++) {
+        int64_t low = R & 127;         /* 0..127 (two's complement ok) */
+        if (low >= 64) low -= 128;     /* balanced: -64..63 */
+        tmp[k] = (int)low;
+        R = (R - low) >> 7;            /* exact */
+    }
+    /* a top carry can leave R = +-1 only when |X| > 2^55 - 2^48*64; we
+     * keep |X| <= 2^55 so fold it into the top digit (then |d_1| <= 64). */
+    tmp[total - 1] += (int)(R * 128);
+    for (int k = 0; k < s; k++) d[k] = tmp[total - 1 - k];
+}
+
+/* C_leaf = split product of column-major m x m A and B (nd diagonals kept). */
+void caps_oracle_split_gemm(int64_t m, const double *A, const double *B, int s, int nd, double *C)
+{
+    int *fa = (int *)malloc((size_t)m * sizeof(int));
+    int *fb = (int *)malloc((size_t)m * sizeof(int));
+    for (int64_t i = 0; i < m; i++) {
+        int E = -100000;
+        for (int64_t k = 0; k < m; k++) { int e = exp_bound(A[i + k * m]); if (e > E) E = e; }
+        fa[i] = (E == -100000) ? 0 : 55 - E;
+    }
+    for (int64_t j = 0; j < m; j++) {
+        int E = -100000;
+        for (int64_t k = 0; k < m; k++) { int e = exp_bound(B[k + j * m]); if (e > E) E = e; }
+        fb[j] = (E == -100000) ? 0 : 55 - E;
+    }
+    int8_t *da = (int8_t *)malloc((size_t)(m * m * s));
+    int8_t *db = (int8_t *)malloc((size_t)(m * m * s));
+    for (int64_t i = 0; i < m; i++)
+        for (int64_t k = 0; k < m; k++) {
+            int d[16];
+            split_digits(A[i + k * m], fa[i], s, d);
+            for (int a = 0; a < s; a++) da[(i * m + k) * s + a] = (int8_t)d[a];
+        }
+    for (int64_t j = 0; j < m; j++)
+        for (int64_t k = 0; k < m; k++) {
+            int d[16];
+            split_digits(B[k + j * m], fb[j], s, d);
+            for (int b = 0; b < s; b++) db[(j * m + k) * s + b] = (int8_t)d[b];
+        }
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t j = 0; j < m; j++) {
+        for (int64_t i = 0; i < m; i++) {
+            int64_t ct[20];
+            for (int t = 0; t < 20; t++) ct[t] = 0;
+            for (int64_t k = 0; k < m; k++) {
+                const int8_t *pa = da + (i * m + k) * s, *pb = db + (j * m + k) * s;
+                for (int a = 0; a < s; a++)
+                    for (int b = 0; b < s; b++)
+                        if (a + b + 2 <= nd + 1) ct[a + b + 2] += (int64_t)pa[a] * pb[b];
+            }
+            int64_t hi = 0, lo = 0;
+            for (int t = 2; t <= 5; t++) hi += ct[t] << (7 * (5 - t));
+            for (int t = 6; t <= 9; t++) lo += ct[t] << (7 * (9 - t));
+            /* value = (hi 2^28 + lo) 2^(7*7) 2^-(fa+fb); one rounding */
+            double v = fma((double)hi, 268435456.0, (double)lo);
+            C[i + j * m] = ldexp(v, 49 - fa[i] - fb[j]);
+        }
+    }
+    free(da); free(db); free(fa); free(fb);
+}
