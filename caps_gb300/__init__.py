@@ -1,0 +1,281 @@
+"""caps_gb300 -- CAPS Strassen multiply on one GB300 GPU.
+
+Python mirror of the reference's multiply interface (multiply.h:13,
+matrix.h:8-16, communication.h:34-35) over the C ABI of libcaps_gb300.so
+(include/caps_gb300.h).  Device arrays are torch CUDA tensors (float64,
+contiguous); host arrays are numpy float64 arrays.  Errors raise CapsError
+carrying the library status; an invalid pattern raises with the reference's
+message "Invalid pattern" (multiply.cpp:100-104).
+
+There is no CPU fallback: if the CUDA library is missing, importing a
+function that needs it raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libcaps_gb300.so")
+
+CAPS_FORM_PLAIN = 0
+CAPS_FORM_SPLIT = 1
+
+STATUS = {
+    0: "CAPS_OK",
+    1: "CAPS_ERR_INVALID_PATTERN",
+    2: "CAPS_ERR_SIZE",
+    3: "CAPS_ERR_BUDGET",
+    4: "CAPS_ERR_CUDA",
+    5: "CAPS_ERR_ALLOC",
+    6: "CAPS_ERR_TIMEOUT",
+    7: "CAPS_ERR_UNSUPPORTED",
+    8: "CAPS_ERR_ARG",
+}
+
+# every extern "C" function of include/caps_gb300.h
+C_ABI_SYMBOLS = [
+    "caps_options_init", "caps_multiply_dev", "caps_multiply_host", "caps_to_caps_layout_dev",
+    "caps_from_caps_layout_dev", "caps_leaf_gemm_dev", "caps_workspace_size", "caps_resolve_pattern",
+    "caps_get_counters", "caps_reset_counters", "caps_set_phase_timing", "caps_multiply_batched_dev",
+    "caps_status_string", "caps_last_cuda_error", "caps_debug_fail_allocations", "caps_release_cache",
+]
+
+
+class CapsError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(message)
+        self.status = status
+        self.name = STATUS.get(status, str(status))
+
+
+class MatDescriptor(ctypes.Structure):
+    """struct MatDescriptor (matrix.h:8-16); one rank: nproc = nprocr = nprocc = nproc_summa = 1."""
+    _fields_ = [("lda", ctypes.c_int), ("nrec", ctypes.c_int), ("nproc", ctypes.c_int),
+                ("nprocr", ctypes.c_int), ("nprocc", ctypes.c_int), ("nproc_summa", ctypes.c_int),
+                ("bs", ctypes.c_int)]
+
+    @classmethod
+    def make(cls, lda: int, nrec: int, bs: int = 1) -> "MatDescriptor":
+        return cls(lda, nrec, 1, 1, 1, 1, bs)
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("form", ctypes.c_int), ("slices", ctypes.c_int), ("diagonals", ctypes.c_int),
+                ("reserved0", ctypes.c_int), ("workspace_limit", ctypes.c_longlong),
+                ("reserved", ctypes.c_longlong * 4)]
+
+
+class Counters(ctypes.Structure):
+    _fields_ = [("additions", ctypes.c_longlong), ("multiplications", ctypes.c_longlong),
+                ("time_add", ctypes.c_double), ("time_mul", ctypes.c_double),
+                ("time_rearrange", ctypes.c_double), ("workspace_peak_bytes", ctypes.c_longlong),
+                ("split_slices", ctypes.c_int), ("split_diagonals", ctypes.c_int),
+                ("kernel_launches", ctypes.c_longlong)]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded libcaps_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libcaps_gb300.so is not built (run caps_gb300/build.py); "
+                              "there is no CPU fallback")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)
+        D = MatDescriptor
+        OP = ctypes.POINTER(Options)
+        L.caps_options_init.argtypes = [OP]
+        L.caps_options_init.restype = None
+        L.caps_multiply_dev.argtypes = [vp, vp, vp, D, ctypes.c_char_p, OP, vp]
+        L.caps_multiply_dev.restype = ctypes.c_int
+        L.caps_multiply_host.argtypes = [dp, dp, dp, D, ctypes.c_char_p, OP]
+        L.caps_multiply_host.restype = ctypes.c_int
+        L.caps_to_caps_layout_dev.argtypes = [vp, vp, D, vp]
+        L.caps_to_caps_layout_dev.restype = ctypes.c_int
+        L.caps_from_caps_layout_dev.argtypes = [vp, vp, D, vp]
+        L.caps_from_caps_layout_dev.restype = ctypes.c_int
+        L.caps_leaf_gemm_dev.argtypes = [vp, vp, vp, ctypes.c_int, OP, vp]
+        L.caps_leaf_gemm_dev.restype = ctypes.c_int
+        L.caps_workspace_size.argtypes = [D, ctypes.c_char_p, OP, ctypes.POINTER(ctypes.c_longlong)]
+        L.caps_workspace_size.restype = ctypes.c_int
+        L.caps_resolve_pattern.argtypes = [D, ctypes.c_char_p, OP, ctypes.c_char_p, ctypes.c_int]
+        L.caps_resolve_pattern.restype = ctypes.c_int
+        L.caps_get_counters.argtypes = [ctypes.POINTER(Counters)]
+        L.caps_get_counters.restype = None
+        L.caps_reset_counters.argtypes = []
+        L.caps_reset_counters.restype = None
+        L.caps_set_phase_timing.argtypes = [ctypes.c_int]
+        L.caps_set_phase_timing.restype = None
+        L.caps_multiply_batched_dev.argtypes = [ctypes.c_int, vp, vp, vp, ctypes.POINTER(ctypes.c_int), OP, vp]
+        L.caps_multiply_batched_dev.restype = ctypes.c_int
+        L.caps_status_string.argtypes = [ctypes.c_int]
+        L.caps_status_string.restype = ctypes.c_char_p
+        L.caps_last_cuda_error.argtypes = []
+        L.caps_last_cuda_error.restype = ctypes.c_char_p
+        L.caps_debug_fail_allocations.argtypes = [ctypes.c_int]
+        L.caps_debug_fail_allocations.restype = None
+        L.caps_release_cache.argtypes = []
+        L.caps_release_cache.restype = None
+        _lib = L
+    return _lib
+
+
+def _check(status: int) -> None:
+    if status != 0:
+        L = lib()
+        msg = L.caps_status_string(status).decode()
+        extra = L.caps_last_cuda_error().decode()
+        if status == 4 and extra:
+            msg = msg + ": " + extra
+        raise CapsError(status, msg)
+
+
+def options(form: int | str = CAPS_FORM_PLAIN, slices: int = 0, diagonals: int = 0,
+            workspace_limit: int = 0) -> Options:
+    if isinstance(form, str):
+        form = {"plain": CAPS_FORM_PLAIN, "split": CAPS_FORM_SPLIT}[form]
+    o = Options()
+    lib().caps_options_init(ctypes.byref(o))
+    o.form, o.slices, o.diagonals, o.workspace_limit = int(form), int(slices), int(diagonals), int(workspace_limit)
+    return o
+
+
+def _pat(pattern):
+    if pattern is None:
+        return None
+    return pattern.encode() if isinstance(pattern, str) else bytes(pattern)
+
+
+def _dev_ptr(t, name):
+    import torch
+    if not (isinstance(t, torch.Tensor) and t.is_cuda):
+        raise TypeError("%s must be a CUDA tensor" % name)
+    if t.dtype != torch.float64 or not t.is_contiguous():
+        raise TypeError("%s must be contiguous float64" % name)
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    return ctypes.c_void_p(int(stream))
+
+
+def multiply(A, B, C, desc: MatDescriptor, pattern=None, form: int | str = CAPS_FORM_PLAIN,
+             slices: int = 0, diagonals: int = 0, workspace_limit: int = 0, stream=None) -> None:
+    """C = A * B for CAPS-layout matrices (multiply.h:13).
+
+    Torch CUDA tensors run asynchronously on `stream` (default: torch's
+    current stream); numpy arrays go through the host entry point, which
+    stages the copies and synchronises.
+    """
+    opt = options(form, slices, diagonals, workspace_limit)
+    if isinstance(A, np.ndarray):
+        for x in (A, B, C):
+            if x.dtype != np.float64 or not x.flags.c_contiguous:
+                raise TypeError("host arrays must be contiguous float64")
+        dp = ctypes.POINTER(ctypes.c_double)
+        _check(lib().caps_multiply_host(A.ctypes.data_as(dp), B.ctypes.data_as(dp), C.ctypes.data_as(dp),
+                                        desc, _pat(pattern), ctypes.byref(opt)))
+        return
+    _check(lib().caps_multiply_dev(_dev_ptr(A, "A"), _dev_ptr(B, "B"), _dev_ptr(C, "C"), desc, _pat(pattern),
+                                   ctypes.byref(opt), _stream_ptr(stream)))
+
+
+def leaf_gemm(A, B, C, m: int, form: int | str = CAPS_FORM_PLAIN, slices: int = 0, diagonals: int = 0,
+              stream=None) -> None:
+    """Base case alone: column-major m x m C = A * B on the device."""
+    opt = options(form, slices, diagonals)
+    _check(lib().caps_leaf_gemm_dev(_dev_ptr(A, "A"), _dev_ptr(B, "B"), _dev_ptr(C, "C"), int(m),
+                                    ctypes.byref(opt), _stream_ptr(stream)))
+
+
+def to_caps_layout(colmajor, out, desc: MatDescriptor, stream=None) -> None:
+    """distributeFrom1Proc (communication.cpp:612-657) on the device."""
+    _check(lib().caps_to_caps_layout_dev(_dev_ptr(colmajor, "colmajor"), _dev_ptr(out, "out"), desc,
+                                         _stream_ptr(stream)))
+
+
+def from_caps_layout(caps, out, desc: MatDescriptor, stream=None) -> None:
+    """collectTo1Proc (communication.cpp:661-708) on the device."""
+    _check(lib().caps_from_caps_layout_dev(_dev_ptr(caps, "caps"), _dev_ptr(out, "out"), desc,
+                                           _stream_ptr(stream)))
+
+
+def multiply_batched(As, Bs, Cs, ns, form: int | str = CAPS_FORM_PLAIN, slices: int = 0, stream=None) -> None:
+    """Independent column-major multiplies of uneven sizes (lists of CUDA tensors)."""
+    count = len(As)
+    arr = ctypes.c_void_p * count
+    pa = arr(*[_dev_ptr(a, "A").value for a in As])
+    pb = arr(*[_dev_ptr(b, "B").value for b in Bs])
+    pc = arr(*[_dev_ptr(c, "C").value for c in Cs])
+    nn = (ctypes.c_int * count)(*[int(n) for n in ns])
+    opt = options(form, slices)
+    _check(lib().caps_multiply_batched_dev(count, ctypes.cast(pa, ctypes.c_void_p), ctypes.cast(pb, ctypes.c_void_p),
+                                           ctypes.cast(pc, ctypes.c_void_p), nn, ctypes.byref(opt),
+                                           _stream_ptr(stream)))
+
+
+def workspace_size(desc: MatDescriptor, pattern=None, form: int | str = CAPS_FORM_PLAIN,
+                   workspace_limit: int = 0) -> int:
+    out = ctypes.c_longlong()
+    opt = options(form, 0, 0, workspace_limit)
+    _check(lib().caps_workspace_size(desc, _pat(pattern), ctypes.byref(opt), ctypes.byref(out)))
+    return out.value
+
+
+def resolve_pattern(desc: MatDescriptor, pattern=None, form: int | str = CAPS_FORM_PLAIN,
+                    workspace_limit: int = 0) -> str:
+    buf = ctypes.create_string_buffer(desc.nrec + 8)
+    opt = options(form, 0, 0, workspace_limit)
+    _check(lib().caps_resolve_pattern(desc, _pat(pattern), ctypes.byref(opt), buf, len(buf)))
+    return buf.value.decode()
+
+
+def counters() -> dict:
+    c = Counters()
+    lib().caps_get_counters(ctypes.byref(c))
+    return {f: getattr(c, f) for f, _ in Counters._fields_}
+
+
+def reset_counters() -> None:
+    lib().caps_reset_counters()
+
+
+def set_phase_timing(enable: bool) -> None:
+    lib().caps_set_phase_timing(1 if enable else 0)
+
+
+def release_cache() -> None:
+    lib().caps_release_cache()
+
+
+def debug_fail_allocations(count: int) -> None:
+    lib().caps_debug_fail_allocations(int(count))
+
+
+@dataclass
+class Flops:
+    effective: float  # 2 n^3
+    actual: float     # additions + multiplications as counters.cpp counts them
+
+
+def flop_counts(n: int, nrec: int) -> Flops:
+    """Effective 2n^3 and the reference's counted flops (counters.cpp:65-69)."""
+    m = n >> nrec
+    adds = 0
+    for l in range(nrec):
+        q = (n >> (l + 1)) ** 2
+        adds += 15 * q * 7 ** l
+    leaves = 7 ** nrec
+    muls = leaves * m ** 3
+    adds += leaves * m ** 3
+    return Flops(2.0 * n ** 3, float(adds + muls))

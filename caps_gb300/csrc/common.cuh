@@ -1,0 +1,101 @@
+// Shared definitions for the CAPS GB300 kernels and host engine.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "../../include/caps_gb300.h"
+
+namespace caps {
+
+// Records the CUDA error text for caps_last_cuda_error().
+void note_cuda_error(cudaError_t e, const char *where);
+
+#define CAPS_CUDA_TRY(expr)                                  \
+    do {                                                     \
+        cudaError_t _e = (expr);                             \
+        if (_e != cudaSuccess) {                             \
+            ::caps::note_cuda_error(_e, #expr);              \
+            return CAPS_ERR_CUDA;                            \
+        }                                                    \
+    } while (0)
+
+#define CAPS_TRY(expr)                                       \
+    do {                                                     \
+        caps_status _s = (expr);                             \
+        if (_s != CAPS_OK) return _s;                        \
+    } while (0)
+
+// Count of kernels this library launched (for the bench's launch count).
+void count_launch(long long n = 1);
+
+// ---------------------------------------------------------------------------
+// Batched elementwise programs over quarter arrays.
+//
+// One Strassen-Winograd node reads the quadrants X11, X21, X12, X22 of its A
+// and B (offsets 0,1,2,3 times q) and forms the operand sums; after the
+// subproducts it forms the C quadrants.  The per-element arithmetic and its
+// order are the reference's (multiply.cpp:409-454 and calcCij :195-210).
+// ---------------------------------------------------------------------------
+enum EwOp : int {
+    // forms T3,T4,T5,T6 from A and S3,S4,S5,S7 from B (8 outputs)
+    EW_FORM_ST = 0,
+    // dst0 = src0 (copy)
+    EW_COPY = 1,
+    // dst0 = src0 + src1 ; dst1 = dst0  (U1 = Q1+Q4 stored in two buffers)
+    EW_ADD_DUP = 2,
+    // dst0 = src0 + src1
+    EW_ADD = 3,
+    // dst0 = src0 - src1
+    EW_SUB = 4,
+    // dst0 = src0 + src2 ; dst1 = src1 + src2   (C22 = U2+Q3 ; U3 = U3+Q3)
+    EW_ADD2 = 5,
+    // calcCij: C11..C22 from Q1..Q7 (7 inputs, 4 outputs)
+    EW_CALC_CIJ = 6,
+};
+
+struct EwTask {
+    const double *src[8];
+    double *dst[8];
+};
+
+// Launches `op` over `count` tasks of q elements each.  `tasks` is a device
+// array.  `vec`: every pointer 16-byte aligned and q even (double2 path).
+cudaError_t launch_elementwise(int op, const EwTask *tasks, int count, int64_t q,
+                               cudaStream_t stream, bool vec);
+cudaError_t launch_elementwise(int op, const EwTask *tasks, int count, int64_t q,
+                               cudaStream_t stream);
+int ew_sources(int op);
+int ew_dests(int op);
+
+// Layout reorder (column-major <-> CAPS layout) for `count` matrices.
+cudaError_t launch_reorder(const double *const *src_dev, double *const *dst_dev, int count,
+                           int64_t n, int nrec, int64_t bs, bool to_caps, cudaStream_t stream);
+cudaError_t launch_reorder_one(const double *src, double *dst, int64_t n, int nrec, int64_t bs,
+                               bool to_caps, cudaStream_t stream);
+
+// ---------------------------------------------------------------------------
+// Base-case GEMMs over a batch of leaves (column-major m x m each).
+// ---------------------------------------------------------------------------
+struct LeafTask {
+    const double *A;
+    const double *B;
+    double *C;
+};
+
+// FP64 DMMA GEMM (mma.sync f64): C = A * B for every task.
+cudaError_t launch_dmma_gemm(const LeafTask *tasks_dev, int count, int m, cudaStream_t stream);
+
+// Split form.  Workspace per leaf: see split_workspace_bytes().
+struct SplitParams {
+    int slices;     // digits per operand, 1..8
+    int diagonals;  // digit-pair diagonals kept, <= 8, >= slices
+};
+size_t split_workspace_bytes(int m, int count, int slices);
+// Computes per-row / per-column scale exponents and the needed digit count.
+cudaError_t launch_split_scan(const LeafTask *tasks_dev, int count, int m, void *workspace,
+                             cudaStream_t stream);
+// Reads back the digits needed (max over the batch) from the scan results.
+cudaError_t split_needed_slices(void *workspace, int count, int m, int *needed, cudaStream_t stream);
+cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, SplitParams p,
+                              void *workspace, unsigned int *status_dev, cudaStream_t stream);
+
+}  // namespace caps

@@ -1,0 +1,743 @@
+// Host engine of the CAPS GB300 multiply: plans the Strassen-Winograd
+// recursion for one GPU and launches the kernels; implements the C ABI of
+// include/caps_gb300.h.
+//
+// Reference structure it replaces (one rank): multiply() multiply.cpp:9-25,
+// multiplyInternal :28-108, strassenDFS :313-455, strassenBFS :212-310,
+// block_multiply :1082-1141, memory budget memory.cpp:4-37, counters
+// counters.cpp.
+//
+// Execution model.  The recursion works on a BATCH of independent
+// same-size products.  A 'b' level forms the operand sums of every product of
+// the batch in one launch and recurses on a batch seven times larger (the 7
+// subproducts run concurrently), then forms C in one launch (calcCij).  A 'd'
+// level forms the operand sums once and recurses seven times on a batch of
+// the same size, folding each subproduct into C as soon as it is ready, in
+// the reference's summation order.  The leaf level runs one batched GEMM
+// launch.  Workspace comes from a stack over one device arena; the plan is
+// built twice (a dry run sizes the arena, then the real one), and all task
+// tables of a call go to the device in one copy.
+#include "common.cuh"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace caps {
+
+// ------------------------------------------------------------------ state
+static thread_local std::string g_last_err;
+static std::recursive_mutex g_mu;
+static long long g_launches = 0;
+static caps_counters g_counters;
+static int g_fail_allocs = 0;
+static bool g_phase_timing = false;
+
+void note_cuda_error(cudaError_t e, const char *where) {
+    g_last_err = std::string(cudaGetErrorString(e)) + " (" + where + ")";
+}
+void count_launch(long long n) { g_launches += n; }
+
+static caps_status dev_malloc(void **p, size_t bytes) {
+    if (g_fail_allocs > 0) {
+        g_fail_allocs--;
+        g_last_err = "device allocation failed (injected)";
+        return CAPS_ERR_ALLOC;
+    }
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        note_cuda_error(e, "cudaMalloc");
+        *p = nullptr;
+        return CAPS_ERR_ALLOC;
+    }
+    return CAPS_OK;
+}
+
+struct DevBuf {
+    char *ptr = nullptr;
+    size_t size = 0;
+    int device = -1;
+};
+
+static caps_status ensure(DevBuf &b, size_t bytes) {
+    int dev = 0;
+    CAPS_CUDA_TRY(cudaGetDevice(&dev));
+    if (b.ptr && b.size >= bytes && b.device == dev) return CAPS_OK;
+    if (b.ptr) {
+        cudaDeviceSynchronize();
+        cudaFree(b.ptr);
+        b.ptr = nullptr;
+        b.size = 0;
+    }
+    size_t want = bytes < 256 ? 256 : bytes;
+    CAPS_TRY(dev_malloc((void **)&b.ptr, want));
+    b.size = want;
+    b.device = dev;
+    return CAPS_OK;
+}
+
+static DevBuf g_arena;   // workspace + task tables
+static DevBuf g_io;      // device copies for caps_multiply_host
+static DevBuf g_status;  // device status words of split kernels
+
+struct PinnedBuf {
+    void *ptr = nullptr;
+    size_t size = 0;
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+};
+static PinnedBuf g_pinned;
+
+static caps_status pinned_reserve(size_t bytes) {
+    if (g_pinned.pending) {
+        CAPS_CUDA_TRY(cudaEventSynchronize(g_pinned.done));
+        g_pinned.pending = false;
+    }
+    if (!g_pinned.done) CAPS_CUDA_TRY(cudaEventCreateWithFlags(&g_pinned.done, cudaEventDisableTiming));
+    if (g_pinned.ptr && g_pinned.size >= bytes) return CAPS_OK;
+    if (g_pinned.ptr) cudaFreeHost(g_pinned.ptr);
+    g_pinned.ptr = nullptr;
+    size_t want = std::max<size_t>(bytes, 1 << 16);
+    CAPS_CUDA_TRY(cudaMallocHost(&g_pinned.ptr, want));
+    g_pinned.size = want;
+    return CAPS_OK;
+}
+
+// ------------------------------------------------------------------ plan
+enum OpKind { K_EW = 0, K_LEAF_DMMA, K_LEAF_SPLIT, K_REORDER_LEAF };
+enum Phase { PH_ADD = 0, PH_MUL = 1, PH_REARRANGE = 2 };
+
+struct Op {
+    int kind;
+    int ew;
+    bool vec;
+    int64_t q;
+    int count;
+    size_t toff;   // task table offset in the blob
+    size_t toff2;  // second table (reorder dst)
+    int m;
+    int bs;
+    bool to_caps;
+    size_t split_off;  // workspace offset of the split scratch
+    SplitParams sp;
+};
+
+struct Prob {
+    const double *A;
+    const double *B;
+    double *C;
+};
+
+struct Builder {
+    std::vector<Op> ops;
+    std::vector<uint8_t> blob;
+    char *ws_base = nullptr;
+    size_t top = 0, peak = 0;
+    int64_t bs = 1;
+    caps_options opt;
+    long long adds = 0, muls = 0;
+    int split_group = 0;
+
+    size_t mark() const { return top; }
+    void release(size_t m) { top = m; }
+    double *alloc(int64_t elems) {
+        size_t off = (top + 255) & ~(size_t)255;
+        top = off + (size_t)elems * sizeof(double);
+        peak = std::max(peak, top);
+        return reinterpret_cast<double *>(ws_base + off);
+    }
+    size_t alloc_bytes(size_t bytes) {
+        size_t off = (top + 255) & ~(size_t)255;
+        top = off + bytes;
+        peak = std::max(peak, top);
+        return off;
+    }
+    template <typename T>
+    size_t table(const std::vector<T> &v) {
+        size_t off = (blob.size() + 63) & ~(size_t)63;
+        blob.resize(off + v.size() * sizeof(T));
+        if (!v.empty()) memcpy(blob.data() + off, v.data(), v.size() * sizeof(T));
+        return off;
+    }
+};
+
+static bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
+
+static void emit_ew(Builder &b, int op, const std::vector<EwTask> &tasks, int64_t q) {
+    bool vec = (q % 2) == 0;
+    int ns = ew_sources(op), nd = ew_dests(op);
+    for (const EwTask &t : tasks) {
+        for (int k = 0; k < ns; k++) vec = vec && aligned16(t.src[k]);
+        for (int k = 0; k < nd; k++) vec = vec && aligned16(t.dst[k]);
+    }
+    Op o{};
+    o.kind = K_EW;
+    o.ew = op;
+    o.vec = vec;
+    o.q = q;
+    o.count = (int)tasks.size();
+    o.toff = b.table(tasks);
+    b.ops.push_back(o);
+}
+
+static void emit_leaf_gemm(Builder &b, const std::vector<Prob> &P, int64_t m) {
+    if (b.opt.form == CAPS_FORM_SPLIT) {
+        // bound split scratch: groups of leaves
+        size_t per = split_workspace_bytes((int)m, 1, 8);
+        size_t cap = (size_t)8 << 30;  // 8 GiB of digit planes per launch group
+        int g = (int)std::max<size_t>(1, std::min<size_t>(P.size(), cap / std::max<size_t>(per, 1)));
+        if (b.split_group > 0) g = std::min(g, b.split_group);
+        for (size_t s = 0; s < P.size(); s += g) {
+            size_t e = std::min(P.size(), s + g);
+            std::vector<LeafTask> t;
+            for (size_t i = s; i < e; i++) t.push_back({P[i].A, P[i].B, P[i].C});
+            Op o{};
+            o.kind = K_LEAF_SPLIT;
+            o.count = (int)t.size();
+            o.m = (int)m;
+            o.toff = b.table(t);
+            size_t mk = b.mark();
+            o.split_off = b.alloc_bytes(split_workspace_bytes((int)m, o.count, 8));
+            b.release(mk);  // scratch is dead once the launch group has run
+            // keep the peak: the alloc above already raised it
+            o.sp.slices = b.opt.slices;
+            o.sp.diagonals = b.opt.diagonals;
+            b.ops.push_back(o);
+        }
+    } else {
+        std::vector<LeafTask> t;
+        for (const Prob &p : P) t.push_back({p.A, p.B, p.C});
+        Op o{};
+        o.kind = K_LEAF_DMMA;
+        o.count = (int)t.size();
+        o.m = (int)m;
+        o.toff = b.table(t);
+        b.ops.push_back(o);
+    }
+}
+
+static void emit_reorder(Builder &b, const std::vector<const double *> &src,
+                         const std::vector<double *> &dst, int64_t m, int64_t bs, bool to_caps) {
+    Op o{};
+    o.kind = K_REORDER_LEAF;
+    o.count = (int)src.size();
+    o.m = (int)m;
+    o.bs = (int)bs;
+    o.to_caps = to_caps;
+    o.toff = b.table(src);
+    o.toff2 = b.table(dst);
+    b.ops.push_back(o);
+}
+
+// block_multiply (multiply.cpp:1082-1141): leaves in bs x bs blocks are
+// repacked to column-major when 1 < bs < m, multiplied, and unpacked.
+static void build_leaf(Builder &b, const std::vector<Prob> &P, int64_t m) {
+    long long m3 = (long long)m * m * m;
+    b.adds += m3 * (long long)P.size();
+    b.muls += m3 * (long long)P.size();
+    if (b.bs == 1 || b.bs == m) {
+        emit_leaf_gemm(b, P, m);
+        return;
+    }
+    size_t mk = b.mark();
+    std::vector<Prob> Q;
+    std::vector<const double *> sa, sb, sc_src;
+    std::vector<double *> da, db, sc_dst;
+    for (const Prob &p : P) {
+        double *w = b.alloc(3 * m * m);
+        Q.push_back({w, w + m * m, w + 2 * m * m});
+        sa.push_back(p.A);
+        da.push_back(w);
+        sb.push_back(p.B);
+        db.push_back(w + m * m);
+        sc_src.push_back(w + 2 * m * m);
+        sc_dst.push_back(p.C);
+    }
+    emit_reorder(b, sa, da, m, b.bs, false);
+    emit_reorder(b, sb, db, m, b.bs, false);
+    emit_leaf_gemm(b, Q, m);
+    emit_reorder(b, sc_src, sc_dst, m, b.bs, true);
+    b.release(mk);
+}
+
+static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, const char *pat) {
+    if (nrec == 0) {
+        build_leaf(b, P, n);
+        return;
+    }
+    const int64_t h = n / 2, q = h * h;
+    const char c = pat[0];
+    b.adds += 15LL * q * (long long)P.size();
+    size_t mk = b.mark();
+    std::vector<EwTask> st(P.size());
+    if (c == 'b' || c == 'B') {
+        // strassenBFS (multiply.cpp:212-310) on one GPU: 7 subproducts as one batch.
+        std::vector<Prob> ch;
+        std::vector<EwTask> cij(P.size());
+        for (size_t i = 0; i < P.size(); i++) {
+            const Prob &p = P[i];
+            const double *A11 = p.A, *A21 = p.A + q, *A12 = p.A + 2 * q, *A22 = p.A + 3 * q;
+            const double *B11 = p.B, *B21 = p.B + q, *B12 = p.B + 2 * q, *B22 = p.B + 3 * q;
+            double *W = b.alloc(15 * q);
+            double *T3 = W, *T4 = W + q, *T5 = W + 2 * q, *T6 = W + 3 * q;
+            double *S3 = W + 4 * q, *S4 = W + 5 * q, *S5 = W + 6 * q, *S7 = W + 7 * q;
+            double *Qv[7];
+            for (int k = 0; k < 7; k++) Qv[k] = W + (8 + k) * q;
+            st[i] = EwTask{{A11, A21, A12, A22, B11, B21, B12, B22}, {T3, T4, T5, T6, S3, S4, S5, S7}};
+            ch.push_back({A11, B11, Qv[0]});
+            ch.push_back({A12, B21, Qv[1]});
+            ch.push_back({T3, S3, Qv[2]});
+            ch.push_back({T4, S4, Qv[3]});
+            ch.push_back({T5, S5, Qv[4]});
+            ch.push_back({T6, B22, Qv[5]});
+            ch.push_back({A22, S7, Qv[6]});
+            EwTask t{};
+            for (int k = 0; k < 7; k++) t.src[k] = Qv[k];
+            t.dst[0] = p.C;          // C11
+            t.dst[1] = p.C + 2 * q;  // C12
+            t.dst[2] = p.C + q;      // C21
+            t.dst[3] = p.C + 3 * q;  // C22
+            cij[i] = t;
+        }
+        emit_ew(b, EW_FORM_ST, st, q);
+        build(b, ch, h, nrec - 1, pat + 1);
+        emit_ew(b, EW_CALC_CIJ, cij, q);
+    } else {
+        // strassenDFS (multiply.cpp:409-454): subproducts in sequence, each
+        // folded into C in the reference's order:
+        //   C11=Q1; U2=U3=C11+Q4; U2+=Q5; C22=U2+Q3, U3+=Q3; C21=U2-Q7;
+        //   C12=U3+Q6; C11+=Q2.
+        struct Nd {
+            const double *A11, *A21, *A12, *A22, *B11, *B21, *B12, *B22;
+            double *C11, *C21, *C12, *C22;
+            double *T3, *T4, *T5, *T6, *S3, *S4, *S5, *S7, *Q, *U2, *U3;
+        };
+        std::vector<Nd> nd(P.size());
+        for (size_t i = 0; i < P.size(); i++) {
+            const Prob &p = P[i];
+            Nd &d = nd[i];
+            d.A11 = p.A; d.A21 = p.A + q; d.A12 = p.A + 2 * q; d.A22 = p.A + 3 * q;
+            d.B11 = p.B; d.B21 = p.B + q; d.B12 = p.B + 2 * q; d.B22 = p.B + 3 * q;
+            d.C11 = p.C; d.C21 = p.C + q; d.C12 = p.C + 2 * q; d.C22 = p.C + 3 * q;
+            double *W = b.alloc(11 * q);
+            d.T3 = W; d.T4 = W + q; d.T5 = W + 2 * q; d.T6 = W + 3 * q;
+            d.S3 = W + 4 * q; d.S4 = W + 5 * q; d.S5 = W + 6 * q; d.S7 = W + 7 * q;
+            d.Q = W + 8 * q; d.U2 = W + 9 * q; d.U3 = W + 10 * q;
+            st[i] = EwTask{{d.A11, d.A21, d.A12, d.A22, d.B11, d.B21, d.B12, d.B22},
+                           {d.T3, d.T4, d.T5, d.T6, d.S3, d.S4, d.S5, d.S7}};
+        }
+        emit_ew(b, EW_FORM_ST, st, q);
+        auto sub = [&](int which) {
+            std::vector<Prob> ch;
+            for (const Nd &d : nd) {
+                switch (which) {
+                    case 1: ch.push_back({d.A11, d.B11, d.C11}); break;
+                    case 2: ch.push_back({d.A12, d.B21, d.Q}); break;
+                    case 3: ch.push_back({d.T3, d.S3, d.Q}); break;
+                    case 4: ch.push_back({d.T4, d.S4, d.Q}); break;
+                    case 5: ch.push_back({d.T5, d.S5, d.Q}); break;
+                    case 6: ch.push_back({d.T6, d.B22, d.Q}); break;
+                    case 7: ch.push_back({d.A22, d.S7, d.Q}); break;
+                }
+            }
+            build(b, ch, h, nrec - 1, pat + 1);
+        };
+        auto comb = [&](int op, auto fill) {
+            std::vector<EwTask> t(nd.size());
+            for (size_t i = 0; i < nd.size(); i++) {
+                t[i] = EwTask{};
+                fill(nd[i], t[i]);
+            }
+            emit_ew(b, op, t, q);
+        };
+        sub(1);
+        sub(4);
+        comb(EW_ADD_DUP, [](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = d.Q; t.dst[0] = d.U2; t.dst[1] = d.U3; });
+        sub(5);
+        comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.U2; t.src[1] = d.Q; t.dst[0] = d.U2; });
+        sub(3);
+        comb(EW_ADD2, [](const Nd &d, EwTask &t) { t.src[0] = d.U2; t.src[1] = d.U3; t.src[2] = d.Q; t.dst[0] = d.C22; t.dst[1] = d.U3; });
+        sub(7);
+        comb(EW_SUB, [](const Nd &d, EwTask &t) { t.src[0] = d.U2; t.src[1] = d.Q; t.dst[0] = d.C21; });
+        sub(6);
+        comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.U3; t.src[1] = d.Q; t.dst[0] = d.C12; });
+        sub(2);
+        comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = d.Q; t.dst[0] = d.C11; });
+    }
+    b.release(mk);
+}
+
+// ------------------------------------------------------------------ checks
+static caps_status check_desc(const caps_desc &d) {
+    if (d.nproc != 1 || d.nprocr != 1 || d.nprocc != 1 || d.nproc_summa != 1)
+        return CAPS_ERR_UNSUPPORTED;
+    if (d.lda <= 0 || d.nrec < 0 || d.bs <= 0 || d.nrec > 24) return CAPS_ERR_SIZE;
+    int64_t unit = ((int64_t)1 << d.nrec) * d.bs;
+    if (d.lda % unit != 0) return CAPS_ERR_SIZE;
+    return CAPS_OK;
+}
+
+static caps_status check_pattern(const caps_desc &d, const char *pat) {
+    if (!pat) return CAPS_OK;
+    for (int l = 0; l < d.nrec; l++) {
+        char c = pat[l];
+        if (c == 0) return CAPS_ERR_INVALID_PATTERN;
+        if (!(c == 'b' || c == 'B' || c == 'd' || c == 'D' || c == 'h' || c == 'H'))
+            return CAPS_ERR_INVALID_PATTERN;
+    }
+    return CAPS_OK;
+}
+
+static caps_options opts_or_default(const caps_options *o) {
+    caps_options r;
+    caps_options_init(&r);
+    if (o) r = *o;
+    return r;
+}
+
+static caps_status check_opts(const caps_options &o) {
+    if (o.form != CAPS_FORM_PLAIN && o.form != CAPS_FORM_SPLIT) return CAPS_ERR_ARG;
+    if (o.slices < 0 || o.slices > 8) return CAPS_ERR_ARG;
+    if (o.diagonals < 0 || o.diagonals > 8) return CAPS_ERR_ARG;
+    return CAPS_OK;
+}
+
+// Bytes of workspace one level's pattern char costs for a batch of `count`.
+static int64_t level_ws(char c, int64_t n, int64_t count) {
+    int64_t q = (n / 2) * (n / 2);
+    return (c == 'b' || c == 'B' ? 15 : 11) * q * 8 * count;
+}
+
+// Chooses a pattern when the caller gives none: 'b' at the deepest levels
+// while the extra workspace fits the budget (batching the subproducts keeps
+// the GPU full), 'd' above (memory-lean), as the -m budget drives the BFS
+// choice in the reference (multiply.cpp:43-66).
+static void auto_pattern(const caps_desc &d, const caps_options &o, char *out) {
+    int r = d.nrec;
+    for (int l = 0; l < r; l++) out[l] = 'd';
+    out[r] = 0;
+    int64_t budget = o.workspace_limit > 0 ? o.workspace_limit : ((int64_t)24 << 30);
+    for (int l = r - 1; l >= 0; l--) {
+        out[l] = 'b';
+        // workspace along the recursion: sum over levels of per-level cost
+        int64_t total = 0, count = 1, n = d.lda;
+        for (int k = 0; k < r; k++) {
+            total += level_ws(out[k], n, count);
+            if (out[k] == 'b' || out[k] == 'B') count *= 7;
+            n /= 2;
+        }
+        if (o.form == CAPS_FORM_SPLIT) total += (int64_t)std::min<size_t>(split_workspace_bytes((int)n, (int)count, 8), (size_t)8 << 30);
+        if (total > budget) {
+            out[l] = 'd';
+            break;
+        }
+    }
+}
+
+struct Planned {
+    Builder b;
+    size_t ws_bytes;
+    size_t table_off;
+    size_t total;
+};
+
+static caps_status plan(const double *A, const double *B, double *C, const caps_desc &d,
+                        const char *pat, const caps_options &o, char *ws_base, Planned &pl) {
+    pl.b = Builder();
+    pl.b.ws_base = ws_base;
+    pl.b.bs = d.bs;
+    pl.b.opt = o;
+    std::vector<Prob> P{{A, B, C}};
+    build(pl.b, P, d.lda, d.nrec, pat);
+    pl.ws_bytes = (pl.b.peak + 255) & ~(size_t)255;
+    pl.table_off = pl.ws_bytes;
+    pl.total = pl.table_off + pl.b.blob.size() + 256;
+    return CAPS_OK;
+}
+
+// ------------------------------------------------------------------ run
+static caps_status run_ops(Planned &pl, cudaStream_t s, double *phase_time) {
+    char *tables = g_arena.ptr + pl.table_off;
+    if (!pl.b.blob.empty()) {
+        CAPS_TRY(pinned_reserve(pl.b.blob.size()));
+        memcpy(g_pinned.ptr, pl.b.blob.data(), pl.b.blob.size());
+        CAPS_CUDA_TRY(cudaMemcpyAsync(tables, g_pinned.ptr, pl.b.blob.size(), cudaMemcpyHostToDevice, s));
+        CAPS_CUDA_TRY(cudaEventRecord(g_pinned.done, s));
+        g_pinned.pending = true;
+    }
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> evphase;
+    for (const Op &o : pl.b.ops) {
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (phase_time) {
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            cudaEventRecord(e0, s);
+        }
+        cudaError_t err = cudaSuccess;
+        int ph = PH_ADD;
+        switch (o.kind) {
+            case K_EW:
+                err = launch_elementwise(o.ew, reinterpret_cast<const EwTask *>(tables + o.toff), o.count, o.q, s, o.vec);
+                ph = PH_ADD;
+                break;
+            case K_LEAF_DMMA:
+                err = launch_dmma_gemm(reinterpret_cast<const LeafTask *>(tables + o.toff), o.count, o.m, s);
+                ph = PH_MUL;
+                break;
+            case K_LEAF_SPLIT: {
+                const LeafTask *t = reinterpret_cast<const LeafTask *>(tables + o.toff);
+                void *ws = g_arena.ptr + o.split_off;
+                err = launch_split_scan(t, o.count, o.m, ws, s);
+                if (err == cudaSuccess)
+                    err = launch_split_gemm(t, o.count, o.m, o.sp, ws, reinterpret_cast<unsigned *>(g_status.ptr), s);
+                ph = PH_MUL;
+                break;
+            }
+            case K_REORDER_LEAF:
+                err = launch_reorder(reinterpret_cast<const double *const *>(tables + o.toff),
+                                     reinterpret_cast<double *const *>(tables + o.toff2), o.count, o.m, 0,
+                                     o.bs, o.to_caps, s);
+                ph = PH_REARRANGE;
+                break;
+        }
+        if (err != cudaSuccess) {
+            note_cuda_error(err, "kernel launch");
+            return CAPS_ERR_CUDA;
+        }
+        if (phase_time) {
+            cudaEventRecord(e1, s);
+            ev.push_back(e0);
+            ev.push_back(e1);
+            evphase.push_back(ph);
+        }
+    }
+    if (phase_time) {
+        CAPS_CUDA_TRY(cudaStreamSynchronize(s));
+        for (size_t i = 0; i < evphase.size(); i++) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]);
+            phase_time[evphase[i]] += ms * 1e-3;
+            cudaEventDestroy(ev[2 * i]);
+            cudaEventDestroy(ev[2 * i + 1]);
+        }
+    }
+    return CAPS_OK;
+}
+
+static caps_status status_buffer() {
+    if (!g_status.ptr) {
+        CAPS_TRY(ensure(g_status, 256));
+        CAPS_CUDA_TRY(cudaMemset(g_status.ptr, 0, 256));
+    }
+    return CAPS_OK;
+}
+
+// Reads (and clears) the device status word of the split kernels, and the
+// digit / diagonal counts the last split launch group used.
+static caps_status check_device_status(cudaStream_t s, const void *last_split_ws) {
+    if (!g_status.ptr) return CAPS_OK;
+    unsigned h = 0;
+    int sd[3] = {0, 0, 0};
+    CAPS_CUDA_TRY(cudaMemcpyAsync(&h, g_status.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    if (last_split_ws)
+        CAPS_CUDA_TRY(cudaMemcpyAsync(sd, last_split_ws, sizeof sd, cudaMemcpyDeviceToHost, s));
+    CAPS_CUDA_TRY(cudaStreamSynchronize(s));
+    g_counters.split_slices = sd[1];
+    g_counters.split_diagonals = sd[2];
+    if (h != 0) {
+        CAPS_CUDA_TRY(cudaMemsetAsync(g_status.ptr, 0, sizeof(unsigned), s));
+        char buf[96];
+        snprintf(buf, sizeof buf, "device wait gave up (status 0x%x)", h);
+        g_last_err = buf;
+        return CAPS_ERR_TIMEOUT;
+    }
+    return CAPS_OK;
+}
+
+static caps_status multiply_dev_locked(const double *A, const double *B, double *C, caps_desc d,
+                                       const char *pattern, const caps_options &o, cudaStream_t s,
+                                       bool sync_status) {
+    CAPS_TRY(check_desc(d));
+    CAPS_TRY(check_pattern(d, pattern));
+    CAPS_TRY(check_opts(o));
+    if (!A || !B || !C) return CAPS_ERR_ARG;
+    char pat[32];
+    if (pattern) {
+        for (int l = 0; l < d.nrec; l++) pat[l] = pattern[l];
+        pat[d.nrec] = 0;
+    } else {
+        auto_pattern(d, o, pat);
+    }
+    Planned pl;
+    CAPS_TRY(plan(A, B, C, d, pat, o, nullptr, pl));
+    if (o.workspace_limit > 0 && (long long)pl.ws_bytes > o.workspace_limit) {
+        g_last_err = "workspace of the pattern exceeds the budget";
+        return CAPS_ERR_BUDGET;
+    }
+    if (o.form == CAPS_FORM_SPLIT) CAPS_TRY(status_buffer());
+    CAPS_TRY(ensure(g_arena, pl.total));
+    CAPS_TRY(plan(A, B, C, d, pat, o, g_arena.ptr, pl));
+    double pt[3] = {0, 0, 0};
+    long long l0 = g_launches;
+    CAPS_TRY(run_ops(pl, s, g_phase_timing ? pt : nullptr));
+    g_counters.additions = pl.b.adds;
+    g_counters.multiplications = pl.b.muls;
+    g_counters.time_add = pt[PH_ADD];
+    g_counters.time_mul = pt[PH_MUL];
+    g_counters.time_rearrange = pt[PH_REARRANGE];
+    g_counters.workspace_peak_bytes = (long long)pl.ws_bytes;
+    g_counters.kernel_launches = g_launches - l0;
+    if (o.form == CAPS_FORM_SPLIT && sync_status) {
+        const void *last = nullptr;
+        for (const Op &op : pl.b.ops)
+            if (op.kind == K_LEAF_SPLIT) last = g_arena.ptr + op.split_off;
+        CAPS_TRY(check_device_status(s, last));
+    }
+    return CAPS_OK;
+}
+
+}  // namespace caps
+
+using namespace caps;
+
+// ======================================================================= ABI
+extern "C" {
+
+void caps_options_init(caps_options *opt) {
+    if (!opt) return;
+    memset(opt, 0, sizeof(*opt));
+    opt->form = CAPS_FORM_PLAIN;
+}
+
+caps_status caps_multiply_dev(const double *A, const double *B, double *C, caps_desc desc,
+                              const char *pattern, const caps_options *opt, void *stream) {
+    std::lock_guard<std::recursive_mutex> g(g_mu);
+    return multiply_dev_locked(A, B, C, desc, pattern, opts_or_default(opt), (cudaStream_t)stream, true);
+}
+
+caps_status caps_multiply_host(const double *A, const double *B, double *C, caps_desc desc,
+                               const char *pattern, const caps_options *opt) {
+    std::lock_guard<std::recursive_mutex> g(g_mu);
+    if (!A || !B || !C) return CAPS_ERR_ARG;
+    CAPS_TRY(check_desc(desc));
+    CAPS_TRY(check_pattern(desc, pattern));
+    size_t nn = (size_t)desc.lda * desc.lda * sizeof(double);
+    size_t slot = (nn + 255) & ~(size_t)255;
+    CAPS_TRY(ensure(g_io, 3 * slot));
+    double *dA = (double *)g_io.ptr, *dB = (double *)(g_io.ptr + slot), *dC = (double *)(g_io.ptr + 2 * slot);
+    cudaStream_t s = 0;
+    CAPS_CUDA_TRY(cudaMemcpyAsync(dA, A, nn, cudaMemcpyHostToDevice, s));
+    CAPS_CUDA_TRY(cudaMemcpyAsync(dB, B, nn, cudaMemcpyHostToDevice, s));
+    CAPS_TRY(multiply_dev_locked(dA, dB, dC, desc, pattern, opts_or_default(opt), s, true));
+    CAPS_CUDA_TRY(cudaMemcpyAsync(C, dC, nn, cudaMemcpyDeviceToHost, s));
+    CAPS_CUDA_TRY(cudaStreamSynchronize(s));
+    return CAPS_OK;
+}
+
+caps_status caps_to_caps_layout_dev(const double *colmajor, double *caps_out, caps_desc desc, void *stream) {
+    CAPS_TRY(check_desc(desc));
+    if (!colmajor || !caps_out) return CAPS_ERR_ARG;
+    CAPS_CUDA_TRY(launch_reorder_one(colmajor, caps_out, desc.lda, desc.nrec, desc.bs, true, (cudaStream_t)stream));
+    return CAPS_OK;
+}
+
+caps_status caps_from_caps_layout_dev(const double *caps_in, double *colmajor, caps_desc desc, void *stream) {
+    CAPS_TRY(check_desc(desc));
+    if (!colmajor || !caps_in) return CAPS_ERR_ARG;
+    CAPS_CUDA_TRY(launch_reorder_one(caps_in, colmajor, desc.lda, desc.nrec, desc.bs, false, (cudaStream_t)stream));
+    return CAPS_OK;
+}
+
+caps_status caps_leaf_gemm_dev(const double *A, const double *B, double *C, int m,
+                               const caps_options *opt, void *stream) {
+    caps_desc d{m, 0, 1, 1, 1, 1, 1};
+    return caps_multiply_dev(A, B, C, d, "", opt, stream);
+}
+
+caps_status caps_workspace_size(caps_desc desc, const char *pattern, const caps_options *opt, long long *bytes) {
+    std::lock_guard<std::recursive_mutex> g(g_mu);
+    CAPS_TRY(check_desc(desc));
+    CAPS_TRY(check_pattern(desc, pattern));
+    if (!bytes) return CAPS_ERR_ARG;
+    caps_options o = opts_or_default(opt);
+    CAPS_TRY(check_opts(o));
+    char pat[32];
+    if (pattern) {
+        for (int l = 0; l < desc.nrec; l++) pat[l] = pattern[l];
+        pat[desc.nrec] = 0;
+    } else {
+        auto_pattern(desc, o, pat);
+    }
+    Planned pl;
+    const double *z = reinterpret_cast<const double *>(256);
+    CAPS_TRY(plan(z, z, const_cast<double *>(z), desc, pat, o, nullptr, pl));
+    *bytes = (long long)pl.ws_bytes;
+    return CAPS_OK;
+}
+
+caps_status caps_resolve_pattern(caps_desc desc, const char *pattern, const caps_options *opt, char *out, int out_len) {
+    CAPS_TRY(check_desc(desc));
+    CAPS_TRY(check_pattern(desc, pattern));
+    if (!out || out_len < desc.nrec + 1) return CAPS_ERR_ARG;
+    caps_options o = opts_or_default(opt);
+    if (pattern) {
+        for (int l = 0; l < desc.nrec; l++) out[l] = pattern[l];
+        out[desc.nrec] = 0;
+    } else {
+        auto_pattern(desc, o, out);
+    }
+    return CAPS_OK;
+}
+
+void caps_get_counters(caps_counters *out) {
+    if (out) *out = g_counters;
+}
+void caps_reset_counters(void) { memset(&g_counters, 0, sizeof(g_counters)); }
+void caps_set_phase_timing(int enable) { g_phase_timing = enable != 0; }
+
+const char *caps_status_string(caps_status s) {
+    switch (s) {
+        case CAPS_OK: return "ok";
+        case CAPS_ERR_INVALID_PATTERN: return "Invalid pattern";
+        case CAPS_ERR_SIZE: return "matrix dimension not divisible by 2^nrec*bs";
+        case CAPS_ERR_BUDGET: return "workspace exceeds the memory budget";
+        case CAPS_ERR_CUDA: return "CUDA error";
+        case CAPS_ERR_ALLOC: return "device allocation failed";
+        case CAPS_ERR_TIMEOUT: return "device wait timed out";
+        case CAPS_ERR_UNSUPPORTED: return "unsupported descriptor (one GPU, one rank)";
+        case CAPS_ERR_ARG: return "invalid argument";
+    }
+    return "unknown status";
+}
+
+const char *caps_last_cuda_error(void) { return g_last_err.c_str(); }
+
+caps_status caps_multiply_batched_dev(int count, const double *const *A, const double *const *B,
+                                      double *const *C, const int *n, const caps_options *opt,
+                                      void *stream) {
+    (void)count; (void)A; (void)B; (void)C; (void)n; (void)opt; (void)stream;
+    return CAPS_ERR_UNSUPPORTED;
+}
+
+void caps_debug_fail_allocations(int count) { g_fail_allocs = count > 0 ? count : 0; }
+
+void caps_release_cache(void) {
+    std::lock_guard<std::recursive_mutex> g(g_mu);
+    cudaDeviceSynchronize();
+    for (DevBuf *b : {&g_arena, &g_io, &g_status}) {
+        if (b->ptr) cudaFree(b->ptr);
+        *b = DevBuf();
+    }
+    if (g_pinned.ptr) cudaFreeHost(g_pinned.ptr);
+    g_pinned.ptr = nullptr;
+    g_pinned.size = 0;
+    g_pinned.pending = false;
+}
+
+}  // extern "C"

@@ -1,0 +1,326 @@
+// Elementwise kernels of the Strassen-Winograd step and the layout reorder.
+//
+// Operand sums and the C combination follow the reference's per-element
+// formulas and evaluation order exactly (multiply.cpp:409-454 for the 'd'
+// step, calcCij multiply.cpp:195-210 for the 'b' step), so for identical
+// subproducts the GPU result is bit-identical to the reference's.
+//
+// All of these are HBM-bound streams: 8 bytes per element per operand.  A
+// block handles one task (blockIdx.y) and a grid-stride range of elements;
+// when every pointer of the launch is 16-byte aligned and q is even, the
+// loop moves double2 vectors.
+#include "common.cuh"
+
+namespace caps {
+
+template <int OP, typename V>
+struct EwBody;
+
+// Winograd operand sums (reference order, multiply.cpp:421-435):
+//   S5 = B22-B12; S3 = B12-B11; S4 = B22-S3; T3 = A21+A22; T5 = A11-A21;
+//   T4 = T3-A11;  T6 = A12-T4;  S7 = S4-B21.
+// src: A11 A21 A12 A22 B11 B21 B12 B22 ; dst: T3 T4 T5 T6 S3 S4 S5 S7
+__device__ __forceinline__ void form_st(double a11, double a21, double a12, double a22,
+                                        double b11, double b21, double b12, double b22,
+                                        double *o) {
+    double s5 = b22 - b12;
+    double s3 = b12 - b11;
+    double s4 = b22 - s3;
+    double t3 = a21 + a22;
+    double t5 = a11 - a21;
+    double t4 = t3 - a11;
+    double t6 = a12 - t4;
+    double s7 = s4 - b21;
+    o[0] = t3; o[1] = t4; o[2] = t5; o[3] = t6;
+    o[4] = s3; o[5] = s4; o[6] = s5; o[7] = s7;
+}
+
+// calcCij (multiply.cpp:195-210).  src Q1..Q7 ; dst C11 C12 C21 C22
+__device__ __forceinline__ void calc_cij(const double *q, double *c) {
+    double c11 = q[0] + q[1];
+    double u1 = q[0] + q[3];
+    double u2 = u1 + q[4];
+    double c21 = u2 - q[6];
+    double c22 = u2 + q[2];
+    double u3 = u1 + q[2];
+    double c12 = u3 + q[5];
+    c[0] = c11; c[1] = c12; c[2] = c21; c[3] = c22;
+}
+
+template <int OP>
+__device__ __forceinline__ void ew_scalar(const EwTask &t, int64_t i) {
+    if (OP == EW_FORM_ST) {
+        double o[8];
+        form_st(t.src[0][i], t.src[1][i], t.src[2][i], t.src[3][i], t.src[4][i], t.src[5][i],
+                t.src[6][i], t.src[7][i], o);
+#pragma unroll
+        for (int k = 0; k < 8; k++) t.dst[k][i] = o[k];
+    } else if (OP == EW_COPY) {
+        t.dst[0][i] = t.src[0][i];
+    } else if (OP == EW_ADD_DUP) {
+        double v = t.src[0][i] + t.src[1][i];
+        t.dst[0][i] = v;
+        t.dst[1][i] = v;
+    } else if (OP == EW_ADD) {
+        t.dst[0][i] = t.src[0][i] + t.src[1][i];
+    } else if (OP == EW_SUB) {
+        t.dst[0][i] = t.src[0][i] - t.src[1][i];
+    } else if (OP == EW_ADD2) {
+        double q = t.src[2][i];
+        double a = t.src[0][i] + q;
+        double b = t.src[1][i] + q;
+        t.dst[0][i] = a;
+        t.dst[1][i] = b;
+    } else if (OP == EW_CALC_CIJ) {
+        double q[7], c[4];
+#pragma unroll
+        for (int k = 0; k < 7; k++) q[k] = t.src[k][i];
+        calc_cij(q, c);
+#pragma unroll
+        for (int k = 0; k < 4; k++) t.dst[k][i] = c[k];
+    }
+}
+
+__device__ __forceinline__ double2 ld2(const double *p, int64_t i) {
+    return __ldcs(reinterpret_cast<const double2 *>(p) + i);
+}
+__device__ __forceinline__ void st2(double *p, int64_t i, double2 v) {
+    __stcs(reinterpret_cast<double2 *>(p) + i, v);
+}
+
+template <int OP>
+__device__ __forceinline__ void ew_vec2(const EwTask &t, int64_t i) {
+    // i indexes double2 vectors; the two lanes are independent elements.
+    if (OP == EW_FORM_ST) {
+        double2 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) v[k] = ld2(t.src[k], i);
+        double o0[8], o1[8];
+        form_st(v[0].x, v[1].x, v[2].x, v[3].x, v[4].x, v[5].x, v[6].x, v[7].x, o0);
+        form_st(v[0].y, v[1].y, v[2].y, v[3].y, v[4].y, v[5].y, v[6].y, v[7].y, o1);
+#pragma unroll
+        for (int k = 0; k < 8; k++) st2(t.dst[k], i, make_double2(o0[k], o1[k]));
+    } else if (OP == EW_CALC_CIJ) {
+        double2 v[7];
+#pragma unroll
+        for (int k = 0; k < 7; k++) v[k] = ld2(t.src[k], i);
+        double q0[7], q1[7], c0[4], c1[4];
+#pragma unroll
+        for (int k = 0; k < 7; k++) { q0[k] = v[k].x; q1[k] = v[k].y; }
+        calc_cij(q0, c0);
+        calc_cij(q1, c1);
+#pragma unroll
+        for (int k = 0; k < 4; k++) st2(t.dst[k], i, make_double2(c0[k], c1[k]));
+    } else if (OP == EW_COPY) {
+        st2(t.dst[0], i, ld2(t.src[0], i));
+    } else if (OP == EW_ADD_DUP) {
+        double2 a = ld2(t.src[0], i), b = ld2(t.src[1], i);
+        double2 r = make_double2(a.x + b.x, a.y + b.y);
+        st2(t.dst[0], i, r);
+        st2(t.dst[1], i, r);
+    } else if (OP == EW_ADD) {
+        double2 a = ld2(t.src[0], i), b = ld2(t.src[1], i);
+        st2(t.dst[0], i, make_double2(a.x + b.x, a.y + b.y));
+    } else if (OP == EW_SUB) {
+        double2 a = ld2(t.src[0], i), b = ld2(t.src[1], i);
+        st2(t.dst[0], i, make_double2(a.x - b.x, a.y - b.y));
+    } else if (OP == EW_ADD2) {
+        double2 a = ld2(t.src[0], i), b = ld2(t.src[1], i), q = ld2(t.src[2], i);
+        double2 r0 = make_double2(a.x + q.x, a.y + q.y);
+        double2 r1 = make_double2(b.x + q.x, b.y + q.y);
+        st2(t.dst[0], i, r0);
+        st2(t.dst[1], i, r1);
+    }
+}
+
+template <int OP, bool VEC>
+__global__ void __launch_bounds__(256) ew_kernel(const EwTask *__restrict__ tasks, int64_t q) {
+    const EwTask t = tasks[blockIdx.y];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    if (VEC) {
+        const int64_t nv = q >> 1;
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride)
+            ew_vec2<OP>(t, i);
+    } else {
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < q; i += stride)
+            ew_scalar<OP>(t, i);
+    }
+}
+
+static int ew_nsrc(int op) {
+    switch (op) {
+        case EW_FORM_ST: return 8;
+        case EW_COPY: return 1;
+        case EW_ADD_DUP: case EW_ADD: case EW_SUB: return 2;
+        case EW_ADD2: return 3;
+        case EW_CALC_CIJ: return 7;
+    }
+    return 0;
+}
+static int ew_ndst(int op) {
+    switch (op) {
+        case EW_FORM_ST: return 8;
+        case EW_ADD_DUP: case EW_ADD2: return 2;
+        case EW_CALC_CIJ: return 4;
+    }
+    return 1;
+}
+int ew_sources(int op) { return ew_nsrc(op); }
+int ew_dests(int op) { return ew_ndst(op); }
+
+template <int OP>
+static void launch_op(bool vec, const EwTask *tasks, int count, int64_t q, cudaStream_t s) {
+    const int threads = 256;
+    int64_t work = vec ? (q >> 1) : q;
+    // enough blocks to cover ~4 waves of the 152 SMs across all tasks
+    int64_t want = (work + threads - 1) / threads;
+    int64_t cap = (int64_t)152 * 8 * 4 / (count > 0 ? count : 1);
+    if (cap < 1) cap = 1;
+    if (want > cap) want = cap;
+    if (want < 1) want = 1;
+    dim3 grid((unsigned)want, (unsigned)count);
+    if (vec)
+        ew_kernel<OP, true><<<grid, threads, 0, s>>>(tasks, q);
+    else
+        ew_kernel<OP, false><<<grid, threads, 0, s>>>(tasks, q);
+}
+
+cudaError_t launch_elementwise(int op, const EwTask *tasks, int count, int64_t q,
+                               cudaStream_t stream, bool vec) {
+    if (count <= 0 || q <= 0) return cudaSuccess;
+    for (int base = 0; base < count; base += 65535) {
+        int c = count - base < 65535 ? count - base : 65535;
+        const EwTask *t = tasks + base;
+        switch (op) {
+            case EW_FORM_ST: launch_op<EW_FORM_ST>(vec, t, c, q, stream); break;
+            case EW_COPY: launch_op<EW_COPY>(vec, t, c, q, stream); break;
+            case EW_ADD_DUP: launch_op<EW_ADD_DUP>(vec, t, c, q, stream); break;
+            case EW_ADD: launch_op<EW_ADD>(vec, t, c, q, stream); break;
+            case EW_SUB: launch_op<EW_SUB>(vec, t, c, q, stream); break;
+            case EW_ADD2: launch_op<EW_ADD2>(vec, t, c, q, stream); break;
+            case EW_CALC_CIJ: launch_op<EW_CALC_CIJ>(vec, t, c, q, stream); break;
+            default: return cudaErrorInvalidValue;
+        }
+        count_launch();
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_elementwise(int op, const EwTask *tasks, int count, int64_t q,
+                               cudaStream_t stream) {
+    return launch_elementwise(op, tasks, count, q, stream, false);
+}
+
+// ---------------------------------------------------------------------------
+// Layout reorder: column-major n x n  <->  CAPS recursive block layout.
+// Restates distributeFrom1ProcRec / collectTo1ProcRec (communication.cpp:
+// 612-704) for one rank: nrec quadrant levels (TL, BL, TR, BR = offsets
+// 0,1,2,3 x quarter), then bs x bs column-major blocks, blocks column-major.
+//
+// One thread per element in CAPS order: consecutive CAPS indices are
+// consecutive rows of one column inside a block (runs of bs, or of the leaf
+// size when bs is 1 or the leaf), so both sides stay coalesced.
+// ---------------------------------------------------------------------------
+struct ReorderGeom {
+    int64_t n, m, mm;   // matrix, leaf, leaf^2
+    int nrec;
+    int bs;             // effective block size (m when bs == 1 or bs == m)
+    int nb;             // blocks per leaf side
+};
+
+__device__ __forceinline__ int64_t caps_to_colmajor_index(const ReorderGeom &g, int64_t idx) {
+    int64_t leaf = idx / g.mm;
+    int64_t off = idx - leaf * g.mm;
+    int64_t r = 0, c = 0;
+    for (int l = 0; l < g.nrec; l++) {
+        int d = (int)((leaf >> (2 * (g.nrec - 1 - l))) & 3);
+        int64_t h = g.n >> (l + 1);
+        r += (d & 1) * h;
+        c += (d >> 1) * h;
+    }
+    int64_t bs2 = (int64_t)g.bs * g.bs;
+    int64_t blk = off / bs2;
+    int64_t w = off - blk * bs2;
+    int64_t bj = blk % g.nb, bi = blk / g.nb;
+    int64_t cc = w / g.bs, rr = w - cc * g.bs;
+    r += bj * g.bs + rr;
+    c += bi * g.bs + cc;
+    return r + c * g.n;
+}
+
+template <bool TO_CAPS>
+__global__ void __launch_bounds__(256) reorder_kernel(const double *const *__restrict__ src,
+                                                      double *const *__restrict__ dst,
+                                                      ReorderGeom g) {
+    const double *s = src[blockIdx.y];
+    double *d = dst[blockIdx.y];
+    const int64_t total = g.n * g.n;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        int64_t cm = caps_to_colmajor_index(g, idx);
+        if (TO_CAPS)
+            d[idx] = __ldcs(s + cm);
+        else
+            d[cm] = __ldcs(s + idx);
+    }
+}
+
+static ReorderGeom make_geom(int64_t n, int nrec, int64_t bs) {
+    ReorderGeom g;
+    g.n = n;
+    g.nrec = nrec;
+    g.m = n >> nrec;
+    g.mm = g.m * g.m;
+    g.bs = (bs == 1 || bs == g.m) ? (int)g.m : (int)bs;
+    g.nb = (int)(g.m / g.bs);
+    return g;
+}
+
+cudaError_t launch_reorder(const double *const *src_dev, double *const *dst_dev, int count,
+                           int64_t n, int nrec, int64_t bs, bool to_caps, cudaStream_t stream) {
+    if (count <= 0) return cudaSuccess;
+    ReorderGeom g = make_geom(n, nrec, bs);
+    int64_t total = n * n;
+    int64_t blocks = (total + 255) / 256;
+    int64_t cap = (int64_t)152 * 8 * 8 / count;
+    if (cap < 1) cap = 1;
+    if (blocks > cap) blocks = cap;
+    dim3 grid((unsigned)blocks, (unsigned)count);
+    if (to_caps)
+        reorder_kernel<true><<<grid, 256, 0, stream>>>(src_dev, dst_dev, g);
+    else
+        reorder_kernel<false><<<grid, 256, 0, stream>>>(src_dev, dst_dev, g);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <bool TO_CAPS>
+__global__ void __launch_bounds__(256) reorder_one_kernel(const double *__restrict__ s,
+                                                          double *__restrict__ d, ReorderGeom g) {
+    const int64_t total = g.n * g.n;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        int64_t cm = caps_to_colmajor_index(g, idx);
+        if (TO_CAPS)
+            d[idx] = __ldcs(s + cm);
+        else
+            d[cm] = __ldcs(s + idx);
+    }
+}
+
+cudaError_t launch_reorder_one(const double *src, double *dst, int64_t n, int nrec, int64_t bs,
+                               bool to_caps, cudaStream_t stream) {
+    ReorderGeom g = make_geom(n, nrec, bs);
+    int64_t total = n * n;
+    int64_t blocks = (total + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    if (to_caps)
+        reorder_one_kernel<true><<<(unsigned)blocks, 256, 0, stream>>>(src, dst, g);
+    else
+        reorder_one_kernel<false><<<(unsigned)blocks, 256, 0, stream>>>(src, dst, g);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace caps

@@ -1,0 +1,692 @@
+// Split form of the base case (Ozaki-style), on tcgen05 tensor cores.
+//
+// The reference multiplies leaves with FP64 dgemm (multiply.cpp:1124,
+// dgemm-blas.cpp:4-13).  Here each leaf product C = A * B (column-major m x m)
+// is computed as follows:
+//
+//  1. scan:     per row i of A the exponent bound E (|a_ij| < 2^E) and the
+//               lowest set bit; the same per column of B.
+//  2. finalize: f_i = 55 - E_i; digits needed = ceil((E - lsb + 1) / 7),
+//               max over the launch group (exact for integer-like inputs).
+//  3. slice:    X = round(a * 2^f) (|X| <= 2^55) is cut into balanced base-128
+//               digits d_1..d_8 (|d| <= 64), the s most significant kept.
+//               Digits are int8 values carried EXACTLY in bf16, written as
+//               pre-tiled UMMA canonical K-major tiles (no swizzle): 8-row x
+//               16-byte core matrices, the two K halves of a row group side
+//               by side (K stride 128 B, row-group stride 256 B), one plane
+//               after another (A: 128 x 16 = 4 KiB, B: 64 x 16 = 2 KiB).
+//  4. gemm:     every digit pair (a, b) with a + b <= nd + 1 is multiplied on
+//               tcgen05.mma kind::f16 (bf16 x bf16 -> f32).  Pairs of one
+//               diagonal t = a + b share one TMEM accumulator (64 columns):
+//               products are <= 2^12, a diagonal has <= 8 pairs, so 512-deep
+//               K chunks sum to <= 2^24 and stay EXACT in fp32.  After each
+//               chunk the epilogue warps move the diagonals into exact int64
+//               sums hi = sum_{t<=5} c_t 2^{7(5-t)}, lo = sum_{t>=6} c_t
+//               2^{7(9-t)}, and at the end C = (hi 2^28 + lo) 2^{49-f_i-g_j}
+//               with one FP64 rounding.
+//
+// GB300 (sm_103a) has no tcgen05 kind::i8, and its FP64 pipe is ~1 TFLOP/s,
+// so the integer slice products go to the bf16 tensor pipe (exact for these
+// ranges) and FP64 work stays O(1) per output element.
+//
+// Each MMA multiplies one A digit plane (128 x 16) by up to four B planes
+// concatenated along N (N = 64 x planes <= 256), writing four consecutive
+// diagonals at once: 12 MMAs per 16-deep K step for s = nd = 8.
+//
+// All mbarrier waits are bounded; a wait that gives up sets a bit in the
+// status word the host reads back (CAPS_ERR_TIMEOUT) and the kernel unwinds,
+// waiting (bounded) for its own copies and MMAs before freeing TMEM.
+#include "common.cuh"
+
+namespace caps {
+
+namespace {
+
+constexpr int TM = 128;         // rows of A per tile (TMEM lanes)
+constexpr int TN = 64;          // columns of B per tile (per diagonal region)
+constexpr int TK = 16;          // K per MMA / per pipeline stage
+constexpr int MAXS = 8;         // max digits
+constexpr int CHUNK = 32;       // K16 steps per exact accumulation chunk (K = 512)
+constexpr int NSTAGE = 4;
+constexpr int A_PLANE_BYTES = TM * TK * 2;  // 4096
+constexpr int B_PLANE_BYTES = TN * TK * 2;  // 2048
+constexpr int STAGE_A = MAXS * A_PLANE_BYTES;
+constexpr int STAGE_B = MAXS * B_PLANE_BYTES;
+constexpr int STAGE_BYTES = STAGE_A + STAGE_B;  // 48 KiB
+constexpr int GEMM_THREADS = 320;               // producer, MMA, 8 epilogue warps
+constexpr uint32_t WAIT_LIMIT = 1u << 25;
+
+struct SplitHdr {
+    int needed;   // max digits needed over the group
+    int s_used;   // written by the gemm for the host
+    int nd_used;
+    int pad[61];
+};
+
+// Workspace of one launch group of `count` leaves:
+//   [header 256 B][scalars of leaf 0..count-1][digit planes of leaf 0..count-1]
+// scalars per leaf: f (A rows), g (B columns), and the scan's exponent / lsb
+// encodings; digits per leaf: A planes then B planes, pre-tiled.
+struct Geo {
+    int m, Mp, Np, Kp, nks, mtiles, ntiles, count;
+    size_t sc_per_leaf, dg_per_leaf, sc_base, dg_base, total;
+    size_t off_fa, off_fb, off_ea, off_la, off_eb, off_lb;  // within a scalar block
+    size_t off_da, off_db;                                  // within a digit block
+};
+
+__host__ __device__ inline Geo make_geo(int m, int count) {
+    Geo g;
+    g.m = m;
+    g.count = count;
+    g.Mp = (m + TM - 1) / TM * TM;
+    g.Np = (m + TN - 1) / TN * TN;
+    g.Kp = (m + TK - 1) / TK * TK;
+    g.nks = g.Kp / TK;
+    g.mtiles = g.Mp / TM;
+    g.ntiles = g.Np / TN;
+    size_t o = 0;
+    g.off_fa = o; o += ((size_t)g.Mp * 4 + 255) & ~(size_t)255;
+    g.off_fb = o; o += ((size_t)g.Np * 4 + 255) & ~(size_t)255;
+    g.off_ea = o; o += ((size_t)g.Mp * 4 + 255) & ~(size_t)255;
+    g.off_la = o; o += ((size_t)g.Mp * 4 + 255) & ~(size_t)255;
+    g.off_eb = o; o += ((size_t)g.Np * 4 + 255) & ~(size_t)255;
+    g.off_lb = o; o += ((size_t)g.Np * 4 + 255) & ~(size_t)255;
+    g.sc_per_leaf = o;
+    o = 0;
+    g.off_da = o; o += ((size_t)g.Mp * g.Kp * 2 * MAXS + 255) & ~(size_t)255;
+    g.off_db = o; o += ((size_t)g.Np * g.Kp * 2 * MAXS + 255) & ~(size_t)255;
+    g.dg_per_leaf = o;
+    g.sc_base = 256;
+    g.dg_base = 256 + (size_t)count * g.sc_per_leaf;
+    g.total = g.dg_base + (size_t)count * g.dg_per_leaf;
+    return g;
+}
+
+__device__ __forceinline__ char *leaf_scalars(char *ws, const Geo &g, int l) {
+    return ws + g.sc_base + (size_t)l * g.sc_per_leaf;
+}
+__device__ __forceinline__ char *leaf_digits(char *ws, const Geo &g, int l) {
+    return ws + g.dg_base + (size_t)l * g.dg_per_leaf;
+}
+
+__device__ __forceinline__ void resolve_sd(const SplitHdr *h, SplitParams p, int &s, int &nd) {
+    int need = h->needed;
+    if (need < 1) need = 1;
+    if (need > MAXS) need = MAXS;
+    s = p.slices > 0 ? p.slices : need;
+    if (s > MAXS) s = MAXS;
+    nd = p.diagonals > 0 ? p.diagonals : (2 * s - 1 < 8 ? 2 * s - 1 : 8);
+    if (nd > 2 * s - 1) nd = 2 * s - 1;  // no digit pair lies beyond diagonal 2s
+    if (nd > 8) nd = 8;
+    if (nd < 1) nd = 1;
+}
+
+// exponent bound E (|x| < 2^E) and lowest set bit of x != 0
+__device__ __forceinline__ void exp_lsb(double x, int &E, int &lsb) {
+    unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    int field = (int)((u >> 52) & 0x7ff);
+    unsigned long long mant = u & 0xFFFFFFFFFFFFFull;
+    if (field == 0) {
+        E = -1022;
+        lsb = -1074 + (__ffsll((long long)mant) - 1);
+    } else {
+        E = field - 1022;
+        unsigned long long M = mant | (1ull << 52);
+        lsb = field - 1075 + (__ffsll((long long)M) - 1);
+    }
+}
+
+}  // namespace
+
+size_t split_workspace_bytes(int m, int count, int /*slices*/) {
+    return make_geo(m, count).total;
+}
+
+// ---------------------------------------------------------------- scan
+// grid.y = 0: A rows, a thread per row and a block per (256 rows, 256-column
+// slab); grid.y = 1: B columns, a warp per column.
+__global__ void __launch_bounds__(256) split_scan_kernel(const LeafTask *__restrict__ tasks,
+                                                         char *__restrict__ ws, Geo g) {
+    const int l = blockIdx.z;
+    const LeafTask t = tasks[l];
+    char *sc = leaf_scalars(ws, g, l);
+    const int64_t M = g.m;
+    constexpr int KSLAB = 256;
+    if (blockIdx.y == 0) {
+        const int64_t rowblocks = (M + 255) / 256;
+        const int64_t slabs = (M + KSLAB - 1) / KSLAB;
+        if ((int64_t)blockIdx.x >= rowblocks * slabs) return;
+        int64_t i = (int64_t)(blockIdx.x % rowblocks) * 256 + threadIdx.x;
+        int64_t k0 = (int64_t)(blockIdx.x / rowblocks) * KSLAB;
+        if (i >= M) return;
+        int64_t k1 = k0 + KSLAB < M ? k0 + KSLAB : M;
+        int emax = -100000, lmin = 100000;
+        for (int64_t k = k0; k < k1; k++) {
+            double x = t.A[i + k * M];
+            if (x != 0.0) {
+                int E, lb;
+                exp_lsb(x, E, lb);
+                emax = E > emax ? E : emax;
+                lmin = lb < lmin ? lb : lmin;
+            }
+        }
+        if (emax > -100000) {
+            atomicMax(reinterpret_cast<int *>(sc + g.off_ea) + i, emax + 4096);
+            atomicMax(reinterpret_cast<int *>(sc + g.off_la) + i, 4096 - lmin);
+        }
+    } else {
+        int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        int64_t j = (int64_t)blockIdx.x * 8 + w;
+        if (j >= M) return;
+        int emax = -100000, lmin = 100000;
+        for (int64_t k = lane; k < M; k += 32) {
+            double x = t.B[k + j * M];
+            if (x != 0.0) {
+                int E, lb;
+                exp_lsb(x, E, lb);
+                emax = E > emax ? E : emax;
+                lmin = lb < lmin ? lb : lmin;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+            lmin = min(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
+        }
+        if (lane == 0 && emax > -100000) {
+            reinterpret_cast<int *>(sc + g.off_eb)[j] = emax + 4096;
+            reinterpret_cast<int *>(sc + g.off_lb)[j] = 4096 - lmin;
+        }
+    }
+}
+
+// f = 55 - E per row / column; digits needed (max over the group)
+__global__ void __launch_bounds__(256) split_finalize_kernel(char *__restrict__ ws, Geo g) {
+    char *leaf = leaf_scalars(ws, g, blockIdx.y);
+    SplitHdr *h = reinterpret_cast<SplitHdr *>(ws);
+    int idx = blockIdx.x * 256 + threadIdx.x;
+    int need = 0;
+    if (idx < g.m) {
+        for (int side = 0; side < 2; side++) {
+            int ee = reinterpret_cast<int *>(leaf + (side ? g.off_eb : g.off_ea))[idx];
+            int le = reinterpret_cast<int *>(leaf + (side ? g.off_lb : g.off_la))[idx];
+            int f = 0;
+            if (ee != 0) {
+                int E = ee - 4096, lsb = 4096 - le;
+                f = 55 - E;
+                int bits = E - lsb + 1;
+                int s = (bits + 6) / 7;
+                need = s > need ? s : need;
+            }
+            reinterpret_cast<int *>(leaf + (side ? g.off_fb : g.off_fa))[idx] = f;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) need = max(need, __shfl_xor_sync(0xffffffffu, need, o));
+    if ((threadIdx.x & 31) == 0 && need > 0) atomicMax(&h->needed, need);
+}
+
+// ---------------------------------------------------------------- slice
+// balanced base-128 digits of round(x 2^f), most significant first
+__device__ __forceinline__ void digits8(double x, int f, int (&d)[8]) {
+    long long R = __double2ll_rn(scalbn(x, f));
+#pragma unroll
+    for (int k = 7; k >= 0; k--) {
+        long long low = R & 127;
+        if (low >= 64) low -= 128;
+        d[k] = (int)low;
+        R = (R - low) >> 7;
+    }
+    d[0] += (int)(R * 128);
+}
+
+// |d| <= 64 has at most 7 significant bits, so the top half of its fp32
+// encoding is its exact bf16 encoding
+__device__ __forceinline__ uint32_t bf16_of_digit(int d) {
+    return __float_as_uint(__int2float_rn(d)) >> 16;
+}
+
+// A side: one thread = one row x 8 k (16 bytes per plane); 256 threads = one
+// 128 x 16 tile.  B side: one thread = one column x 8 k; 256 threads = two
+// 64 x 16 tiles.
+__global__ void __launch_bounds__(256) split_slice_kernel(const LeafTask *__restrict__ tasks, int m,
+                                                          char *__restrict__ ws, Geo g, SplitParams p) {
+    const LeafTask t = tasks[blockIdx.z];
+    char *sc = leaf_scalars(ws, g, blockIdx.z);
+    char *dg = leaf_digits(ws, g, blockIdx.z);
+    int s, nd;
+    resolve_sd(reinterpret_cast<const SplitHdr *>(ws), p, s, nd);
+    const int64_t M = m;
+    const int tid = threadIdx.x;
+    int64_t tile = blockIdx.x;
+    const int64_t atiles = (int64_t)g.mtiles * g.nks;
+    if (blockIdx.y == 0) {
+        if (tile >= atiles) return;
+        int mt = (int)(tile / g.nks), ks = (int)(tile % g.nks);
+        int r = tid & 127, kg = tid >> 7;
+        int64_t i = (int64_t)mt * TM + r;
+        int64_t k0 = (int64_t)ks * TK + kg * 8;
+        int f = i < M ? reinterpret_cast<const int *>(sc + g.off_fa)[i] : 0;
+        uint32_t packed[MAXS][4];
+#pragma unroll
+        for (int pl = 0; pl < MAXS; pl++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) packed[pl][q] = 0;
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            int64_t k = k0 + e;
+            double x = (i < M && k < M) ? t.A[i + k * M] : 0.0;
+            int d[8];
+            digits8(x, f, d);
+#pragma unroll
+            for (int pl = 0; pl < MAXS; pl++) packed[pl][e >> 1] |= bf16_of_digit(d[pl]) << (16 * (e & 1));
+        }
+        char *base = dg + g.off_da + (size_t)(mt * g.nks + ks) * s * A_PLANE_BYTES;
+        size_t off = (size_t)(r >> 3) * 256 + (size_t)kg * 128 + (size_t)(r & 7) * 16;
+        for (int pl = 0; pl < s; pl++)
+            *reinterpret_cast<uint4 *>(base + (size_t)pl * A_PLANE_BYTES + off) =
+                make_uint4(packed[pl][0], packed[pl][1], packed[pl][2], packed[pl][3]);
+    } else {
+        int64_t btiles = (int64_t)g.ntiles * g.nks;
+        int64_t bt = tile * 2 + (tid >> 7);
+        if (bt >= btiles) return;
+        int nt = (int)(bt / g.nks), ks = (int)(bt % g.nks);
+        int c = tid & 63, kg = (tid >> 6) & 1;
+        int64_t j = (int64_t)nt * TN + c;
+        int64_t k0 = (int64_t)ks * TK + kg * 8;
+        int f = j < M ? reinterpret_cast<const int *>(sc + g.off_fb)[j] : 0;
+        uint32_t packed[MAXS][4];
+#pragma unroll
+        for (int pl = 0; pl < MAXS; pl++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) packed[pl][q] = 0;
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            int64_t k = k0 + e;
+            double x = (j < M && k < M) ? t.B[k + j * M] : 0.0;
+            int d[8];
+            digits8(x, f, d);
+#pragma unroll
+            for (int pl = 0; pl < MAXS; pl++) packed[pl][e >> 1] |= bf16_of_digit(d[pl]) << (16 * (e & 1));
+        }
+        char *base = dg + g.off_db + (size_t)(nt * g.nks + ks) * s * B_PLANE_BYTES;
+        for (int pl = 0; pl < s; pl++) {
+            size_t off = (size_t)pl * B_PLANE_BYTES + (size_t)(c >> 3) * 256 + (size_t)kg * 128 +
+                         (size_t)(c & 7) * 16;
+            *reinterpret_cast<uint4 *>(base + off) =
+                make_uint4(packed[pl][0], packed[pl][1], packed[pl][2], packed[pl][3]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- gemm
+namespace {
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait: false (and a status bit) if the phase never completes
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned *status,
+                                          unsigned code) {
+    for (uint32_t it = 0; it < WAIT_LIMIT; it++) {
+        if (mbar_try(bar, parity)) return true;
+        if (it > 64) __nanosleep(it > 4096 ? 256 : 32);
+    }
+    atomicOr(status, code);
+    return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes,
+                                         uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            dst),
+        "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+
+// UMMA shared-memory descriptor, K-major, no swizzle.
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
+    return d;                // base offset 0, swizzle none
+}
+
+// instruction descriptor: kind::f16, A=B=bf16, D=f32, K-major, M x N
+__device__ __forceinline__ uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                     uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+          "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+          "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+          "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// issues MMAs of A plane a (1-based) against B planes covering diagonal
+// regions [ra, rb] (region r = a + j - 2), four planes per instruction
+__device__ __forceinline__ void issue_range(uint32_t tmem, uint32_t a_base, uint32_t b_base,
+                                            int a, int ra, int rb, uint32_t acc) {
+    for (int r = ra; r <= rb; r += 4) {
+        int cnt = rb - r + 1 < 4 ? rb - r + 1 : 4;
+        int j0 = r - (a - 1) + 1;
+        // K-direction core-matrix stride (LBO) 128 B, M/N-direction (SBO) 256 B
+        uint64_t ad = sdesc(a_base + (uint32_t)(a - 1) * A_PLANE_BYTES, 128, 256);
+        uint64_t bd = sdesc(b_base + (uint32_t)(j0 - 1) * B_PLANE_BYTES, 128, 256);
+        umma(tmem + (uint32_t)(TN * r), ad, bd, idesc_bf16(TM, TN * cnt), acc);
+    }
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
+    split_gemm_kernel(const LeafTask *__restrict__ tasks, int count, char *__restrict__ ws, Geo g,
+                      SplitParams p, unsigned *__restrict__ status) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char *stA = smem;                      // NSTAGE x STAGE_A
+    unsigned char *stB = smem + NSTAGE * STAGE_A;   // NSTAGE x STAGE_B
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + NSTAGE * STAGE_BYTES);
+    // bars: full[NSTAGE], empty[NSTAGE], tfull, tempty, final
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * NSTAGE + 3);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int s, nd;
+    resolve_sd(reinterpret_cast<const SplitHdr *>(ws), p, s, nd);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        SplitHdr *h = reinterpret_cast<SplitHdr *>(ws);
+        h->s_used = s;
+        h->nd_used = nd;
+    }
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + NSTAGE);
+    const uint32_t tfull = smem_u32(bars + 2 * NSTAGE), tempty = smem_u32(bars + 2 * NSTAGE + 1);
+    const uint32_t finalb = smem_u32(bars + 2 * NSTAGE + 2);
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < NSTAGE; i++) {
+            mbar_init(full0 + 8 * i, 1);
+            mbar_init(empty0 + 8 * i, 1);
+        }
+        mbar_init(tfull, 1);
+        mbar_init(tempty, 8);
+        mbar_init(finalb, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
+                         smem_u32(tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    const int64_t tiles_per_leaf = (int64_t)g.mtiles * g.ntiles;
+    const int64_t total = tiles_per_leaf * count;
+    const uint32_t bytesA = (uint32_t)s * A_PLANE_BYTES, bytesB = (uint32_t)s * B_PLANE_BYTES;
+    const int nchunks = (g.nks + CHUNK - 1) / CHUNK;
+
+    if (warp == 0) {
+        // ------------------------------------------------ producer
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            bool ok = true;
+            uint32_t armed[NSTAGE] = {0, 0, 0, 0};  // 1 + phase of the last arm
+            for (int64_t tile = blockIdx.x; tile < total && ok; tile += gridDim.x) {
+                int leafi = (int)(tile / tiles_per_leaf);
+                int64_t rem = tile % tiles_per_leaf;
+                int mt = (int)(rem / g.ntiles), nt = (int)(rem % g.ntiles);
+                const char *dg = leaf_digits(ws, g, leafi);
+                const char *srcA = dg + g.off_da + (size_t)mt * g.nks * bytesA;
+                const char *srcB = dg + g.off_db + (size_t)nt * g.nks * bytesB;
+                for (int ks = 0; ks < g.nks; ks++) {
+                    if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, status, 1u)) { ok = false; break; }
+                    mbar_expect_tx(full0 + 8 * stage, bytesA + bytesB);
+                    bulk_g2s(smem_u32(stA + stage * STAGE_A), srcA + (size_t)ks * bytesA, bytesA,
+                             full0 + 8 * stage);
+                    bulk_g2s(smem_u32(stB + stage * STAGE_B), srcB + (size_t)ks * bytesB, bytesB,
+                             full0 + 8 * stage);
+                    armed[stage] = 1 + phase;
+                    if (++stage == NSTAGE) { stage = 0; phase ^= 1; }
+                }
+            }
+            // drain: every armed stage's copies must land before exit
+            for (int i = 0; i < NSTAGE; i++)
+                if (armed[i]) mbar_wait(full0 + 8 * i, armed[i] - 1, status, 2u);
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0, chunk_ctr = 0;
+            bool ok = true;
+            for (int64_t tile = blockIdx.x; tile < total && ok; tile += gridDim.x) {
+                for (int ch = 0; ch < nchunks && ok; ch++) {
+                    if (!mbar_wait(tempty, (chunk_ctr & 1) ^ 1, status, 4u)) { ok = false; break; }
+                    tc_fence_after();
+                    int ks0 = ch * CHUNK, ks1 = ks0 + CHUNK < g.nks ? ks0 + CHUNK : g.nks;
+                    for (int ks = ks0; ks < ks1; ks++) {
+                        if (!mbar_wait(full0 + 8 * stage, phase, status, 8u)) { ok = false; break; }
+                        tc_fence_after();
+                        uint32_t a_base = smem_u32(stA + stage * STAGE_A);
+                        uint32_t b_base = smem_u32(stB + stage * STAGE_B);
+                        int init_hi = (ks == ks0) ? -1 : 1000;
+                        for (int a = 1; a <= s; a++) {
+                            int jmax = s < nd + 1 - a ? s : nd + 1 - a;
+                            if (jmax < 1) break;
+                            int rlo = a - 1, rhi = a - 1 + jmax - 1;
+                            int m1 = rhi < init_hi ? rhi : init_hi;
+                            if (rlo <= m1) issue_range(tmem, a_base, b_base, a, rlo, m1, 1u);
+                            int f0 = rlo > init_hi + 1 ? rlo : init_hi + 1;
+                            if (f0 <= rhi) issue_range(tmem, a_base, b_base, a, f0, rhi, 0u);
+                            if (rhi > init_hi) init_hi = rhi;
+                        }
+                        umma_commit(empty0 + 8 * stage);
+                        if (++stage == NSTAGE) { stage = 0; phase ^= 1; }
+                    }
+                    if (!ok) break;
+                    umma_commit(tfull);
+                    chunk_ctr++;
+                }
+            }
+            // all issued MMAs complete before TMEM is released
+            umma_commit(finalb);
+            mbar_wait(finalb, 0, status, 16u);
+        }
+    } else {
+        // ------------------------------------------------ epilogue (8 warps)
+        const int quarter = warp & 3;          // TMEM lanes 32*quarter..
+        const int colhalf = (warp - 2) >> 2;   // columns 32*colhalf.. of each region
+        uint32_t chunk_ctr = 0;
+        bool ok = true;
+        for (int64_t tile = blockIdx.x; tile < total && ok; tile += gridDim.x) {
+            int leafi = (int)(tile / tiles_per_leaf);
+            int64_t rem = tile % tiles_per_leaf;
+            int mt = (int)(rem / g.ntiles), nt = (int)(rem % g.ntiles);
+            long long hi[32], lo[32];
+#pragma unroll
+            for (int c = 0; c < 32; c++) hi[c] = lo[c] = 0;
+            for (int ch = 0; ch < nchunks; ch++) {
+                // warp-uniform: tcgen05.ld below is .sync.aligned
+                bool got = mbar_wait(tfull, chunk_ctr & 1, status, 32u);
+                if (!__all_sync(0xffffffffu, got)) { ok = false; break; }
+                tc_fence_after();
+                for (int r = 0; r < nd; r++) {
+                    uint32_t v[32];
+                    uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(TN * r + 32 * colhalf);
+                    tmem_ld32(taddr, v);
+                    const int t = r + 2;
+                    if (t <= 5) {
+                        const int sh = 7 * (5 - t);
+#pragma unroll
+                        for (int c = 0; c < 32; c++)
+                            hi[c] += (long long)__float2int_rn(__uint_as_float(v[c])) << sh;
+                    } else {
+                        const int sh = 7 * (9 - t);
+#pragma unroll
+                        for (int c = 0; c < 32; c++)
+                            lo[c] += (long long)__float2int_rn(__uint_as_float(v[c])) << sh;
+                    }
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(tempty);
+                chunk_ctr++;
+            }
+            if (!ok) break;
+            // C = (hi 2^28 + lo) 2^(49 - f_i - g_j), one rounding
+            const char *leaf = leaf_scalars(ws, g, leafi);
+            const int64_t M = g.m;
+            int64_t i = (int64_t)mt * TM + quarter * 32 + lane;
+            if (i < M) {
+                int fa = reinterpret_cast<const int *>(leaf + g.off_fa)[i];
+                const int *fbp = reinterpret_cast<const int *>(leaf + g.off_fb);
+                double *C = tasks[leafi].C;
+#pragma unroll
+                for (int c = 0; c < 32; c++) {
+                    int64_t j = (int64_t)nt * TN + 32 * colhalf + c;
+                    if (j < M) {
+                        double v = fma((double)hi[c], 268435456.0, (double)lo[c]);
+                        C[i + j * M] = ldexp(v, 49 - fa - fbp[j]);
+                    }
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+    }
+}
+
+static int g_num_sms = 0;
+
+cudaError_t launch_split_scan(const LeafTask *tasks_dev, int count, int m, void *workspace,
+                              cudaStream_t stream) {
+    Geo g = make_geo(m, count);
+    cudaError_t e = cudaMemsetAsync(workspace, 0, g.dg_base, stream);
+    if (e != cudaSuccess) return e;
+    int64_t ablocks = ((int64_t)(m + 255) / 256) * ((m + 255) / 256);
+    int64_t bblocks = (m + 7) / 8;
+    int64_t gx = ablocks > bblocks ? ablocks : bblocks;
+    for (int base = 0; base < count; base += 65535) {
+        int c = count - base < 65535 ? count - base : 65535;
+        Geo gb = g;
+        gb.sc_base = g.sc_base + (size_t)base * g.sc_per_leaf;
+        dim3 grid((unsigned)gx, 2, (unsigned)c);
+        split_scan_kernel<<<grid, 256, 0, stream>>>(tasks_dev + base, (char *)workspace, gb);
+        count_launch();
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
+                              unsigned int *status_dev, cudaStream_t stream) {
+    Geo g = make_geo(m, count);
+    char *ws = (char *)workspace;
+    cudaError_t e;
+    {
+        dim3 grid((unsigned)((m + 255) / 256), (unsigned)count);
+        split_finalize_kernel<<<grid, 256, 0, stream>>>(ws, g);
+        count_launch();
+    }
+    {
+        int64_t atiles = (int64_t)g.mtiles * g.nks;
+        int64_t btiles2 = ((int64_t)g.ntiles * g.nks + 1) / 2;
+        int64_t gx = atiles > btiles2 ? atiles : btiles2;
+        dim3 grid((unsigned)gx, 2, (unsigned)count);
+        split_slice_kernel<<<grid, 256, 0, stream>>>(tasks_dev, m, ws, g, p);
+        count_launch();
+    }
+    if (g_num_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_num_sms <= 0) g_num_sms = 152;
+    }
+    size_t smem = (size_t)NSTAGE * STAGE_BYTES + 1024 + 256;
+    e = cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int64_t total = (int64_t)g.mtiles * g.ntiles * count;
+    int grid = (int)(total < g_num_sms ? total : g_num_sms);
+    split_gemm_kernel<<<grid, GEMM_THREADS, smem, stream>>>(tasks_dev, count, ws, g, p, status_dev);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t split_needed_slices(void *workspace, int, int, int *needed, cudaStream_t stream) {
+    SplitHdr h;
+    cudaError_t e = cudaMemcpyAsync(&h, workspace, sizeof(int) * 3, cudaMemcpyDeviceToHost, stream);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(stream);
+    if (needed) *needed = h.needed;
+    return e;
+}
+
+}  // namespace caps

@@ -1,0 +1,93 @@
+/*
+ * caps_compat.h -- the CAPS reference's C++ interface, served by
+ * libcaps_gb300.so on one GPU.  Same names, argument meaning and (C++)
+ * linkage as the reference headers, so code written against CAPS links
+ * against this library instead of multiply.o / communication.o / memory.o /
+ * counters.o / matrix.o / library.o.
+ *
+ *   multiply            multiply.h:13       (multiply.cpp:9-25)
+ *   MatDescriptor       matrix.h:8-16       DESC_SIZE matrix.h:18
+ *   numEntriesPerProc   matrix.h:47         (matrix.cpp:9-12)
+ *   verifyDescriptor    matrix.h:46         (matrix.cpp:3-7)
+ *   allocate, deallocate, enoughMemory, setAvailableMemory, getMaxUsedMemory
+ *                       memory.h:10-14      (memory.cpp)
+ *   initCommunication, initCommunicationAlt, getRank, getComm,
+ *   getLog7nProcs, getPFactor, distributeFrom1Proc, collectTo1Proc
+ *                       communication.h:10-17,34-35
+ *   initTimers, startTimer, stopTimer, printCounters, increase*
+ *                       counters.h:5-21
+ *   read_timer          library.h:8          SEVEN library.h:5
+ *
+ * Differences, all forced by one GPU per process:
+ *   - one rank: getRank() = 0, getLog7nProcs() = 0, getPFactor() = 1;
+ *   - allocate() returns page-locked host memory so multiply() stages its
+ *     copies at full PCIe/C2C speed (falls back to malloc);
+ *   - multiply() copies A, B to the GPU, runs the Strassen recursion there
+ *     and copies C back; the form (FP64 or split) is chosen with
+ *     caps_compat_set_form();
+ *   - a bad pattern prints "Invalid pattern" and exits(-1) as the reference
+ *     does (multiply.cpp:100-104).
+ */
+#ifndef CAPS_COMPAT_H
+#define CAPS_COMPAT_H
+
+struct MatDescriptor {
+    int lda;
+    int nrec;
+    int nproc;
+    int nprocr;
+    int nprocc;
+    int nproc_summa;
+    int bs;
+};
+
+const int DESC_SIZE = 7;
+const int SEVEN = 7;
+
+void multiply(double *A, double *B, double *C, MatDescriptor desc, char *pattern = 0);
+
+void verifyDescriptor(MatDescriptor desc);
+long long numEntriesPerProc(MatDescriptor desc);
+
+double *allocate(long long s);
+void deallocate(double *A, long long s);
+bool enoughMemory(long long memNeeded);
+void setAvailableMemory(long long am);
+double getMaxUsedMemory();
+
+void initCommunication(int *argc, char ***argv, int randomize = 0);
+void initCommunicationAlt(int *argc, char ***argv, int randomize = 0);
+int getRank();
+int getLog7nProcs();
+int getPFactor();
+void distributeFrom1Proc(MatDescriptor desc, double *O, double *I);
+void collectTo1Proc(MatDescriptor desc, double *O, double *I);
+
+void increaseAdditions(long long n);
+void increaseMultiplications(long long n);
+void increaseMessages(long long n);
+void increaseWords(long long n);
+void setExecutionType(int nrec, const char *type);
+void initTimers();
+void startTimer(int type);
+void stopTimer(int type);
+const int TIMER_COMM = 0;
+const int TIMER_ADD = 1;
+const int TIMER_MUL = 2;
+const int TIMER_REARRANGE = 3;
+const int TIMER_COMM_SUMMA = 4;
+const int NUM_TIMERS = 5;
+void printCounters(double t, MatDescriptor desc);
+void printCounters(MatDescriptor desc);
+
+double read_timer();
+
+/* GB300 additions (no reference counterpart). */
+extern "C" {
+/* form: 0 = FP64 (plain), 1 = split; slices 0 = automatic */
+void caps_compat_set_form(int form, int slices);
+/* returns the status of the last multiply() (caps_status) */
+int caps_compat_last_status(void);
+}
+
+#endif

@@ -1,0 +1,150 @@
+/*
+ * caps_gb300.h -- C ABI of the GB300 CAPS Strassen multiply library
+ * (libcaps_gb300.so).  Plain pointers and sizes only; a stream is passed as
+ * `void *` holding a cudaStream_t (NULL = the legacy default stream).
+ *
+ * Matrices are n x n float64 in CAPS's recursive block layout: `nrec` levels
+ * of quadrants stored in the order 11, 21, 12, 22, then bs x bs blocks,
+ * column-major both inside a block and between blocks (matrix.h:20-44).
+ * With bs = 1 a leaf is a plain column-major (n/2^nrec)^2 matrix.
+ *
+ * Every entry point returns a caps_status; nothing calls exit().
+ */
+#ifndef CAPS_GB300_H
+#define CAPS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Mirrors struct MatDescriptor (matrix.h:8-16), same field order. */
+typedef struct caps_desc {
+    int lda;          /* matrix dimension n */
+    int nrec;         /* recursive Strassen steps */
+    int nproc;        /* must be 1: one GPU holds the whole matrix */
+    int nprocr;       /* must be 1 */
+    int nprocc;       /* must be 1 */
+    int nproc_summa;  /* must be 1 */
+    int bs;           /* leaf block size; lda % (2^nrec * bs) == 0 */
+} caps_desc;
+
+typedef enum caps_status {
+    CAPS_OK = 0,
+    CAPS_ERR_INVALID_PATTERN = 1, /* a pattern char other than b/B/d/D/h/H, or too short */
+    CAPS_ERR_SIZE = 2,            /* lda not divisible by 2^nrec*bs, or n <= 0 */
+    CAPS_ERR_BUDGET = 3,          /* workspace the pattern needs exceeds the -m budget */
+    CAPS_ERR_CUDA = 4,            /* a CUDA runtime call failed */
+    CAPS_ERR_ALLOC = 5,           /* device memory allocation failed */
+    CAPS_ERR_TIMEOUT = 6,         /* a bounded device-side wait gave up */
+    CAPS_ERR_UNSUPPORTED = 7,     /* multi-rank descriptor, or no sm_103 device */
+    CAPS_ERR_ARG = 8              /* NULL pointer or out-of-range option */
+} caps_status;
+
+/* Base-case arithmetic. */
+typedef enum caps_form {
+    CAPS_FORM_PLAIN = 0, /* FP64 throughout, base case on FP64 DMMA tensor cores */
+    CAPS_FORM_SPLIT = 1  /* base case split into int8-valued digit slices with
+                            per-row / per-column power-of-two scaling, exact
+                            integer slice products on tcgen05, FP64 recombine */
+} caps_form;
+
+typedef struct caps_options {
+    int form;                  /* caps_form */
+    int slices;                /* split form: digits per operand, 0 = automatic, 1..8 */
+    int diagonals;             /* split form: digit-pair diagonals kept, 0 = automatic */
+    int reserved0;
+    long long workspace_limit; /* bytes of device workspace allowed (-m); <= 0: no limit */
+    long long reserved[4];
+} caps_options;
+
+/* Fills *opt with defaults (plain form, automatic slices, no limit). */
+void caps_options_init(caps_options *opt);
+
+/* C = A * B on device-resident CAPS-layout matrices (the `multiply()` of
+ * multiply.h:13, multiply.cpp:9-25, with device pointers and a stream).
+ * pattern: one char per level ('b'/'B' = the 7 subproducts run concurrently
+ * in one launch, 'd'/'D' = in sequence, 'h'/'H' = 'd' on one GPU), or NULL
+ * to let the library choose.  Asynchronous on `stream`. */
+caps_status caps_multiply_dev(const double *A, const double *B, double *C, caps_desc desc,
+                              const char *pattern, const caps_options *opt, void *stream);
+
+/* Same, on host arrays: copies A, B to the device, multiplies, copies C back
+ * and synchronises.  Replaces the body of multiply() for host callers. */
+caps_status caps_multiply_host(const double *A, const double *B, double *C, caps_desc desc,
+                               const char *pattern, const caps_options *opt);
+
+/* Column-major n x n (ld = n) -> CAPS layout, on the device.
+ * Replaces distributeFrom1Proc (communication.cpp:612-657) for one rank. */
+caps_status caps_to_caps_layout_dev(const double *colmajor, double *caps, caps_desc desc,
+                                    void *stream);
+
+/* CAPS layout -> column-major n x n, on the device.
+ * Replaces collectTo1Proc (communication.cpp:661-708) for one rank. */
+caps_status caps_from_caps_layout_dev(const double *caps, double *colmajor, caps_desc desc,
+                                      void *stream);
+
+/* Base case alone: C = A * B for column-major m x m device matrices in the
+ * given form (block_multiply -> square_dgemm_zero, multiply.cpp:1082-1141,
+ * dgemm-blas.cpp:4-13). */
+caps_status caps_leaf_gemm_dev(const double *A, const double *B, double *C, int m,
+                               const caps_options *opt, void *stream);
+
+/* Workspace bytes caps_multiply_dev needs for (desc, pattern, opt). */
+caps_status caps_workspace_size(caps_desc desc, const char *pattern, const caps_options *opt,
+                                long long *bytes);
+
+/* The pattern the library would run for (desc, pattern, opt): one char per
+ * level written to out (at least desc.nrec + 1 bytes). */
+caps_status caps_resolve_pattern(caps_desc desc, const char *pattern, const caps_options *opt,
+                                 char *out, int out_len);
+
+/* Counters of the last multiply on this thread, as counters.cpp counts them:
+ * additions (element ops, incl. base-case m^3), multiplications (m^3 per
+ * leaf), and device times in seconds of the add / multiply / reorder phases
+ * (CUDA events; 0 unless caps_set_phase_timing(1)). */
+typedef struct caps_counters {
+    long long additions;
+    long long multiplications;
+    double time_add;
+    double time_mul;
+    double time_rearrange;
+    long long workspace_peak_bytes;
+    int split_slices;        /* digits used by the last split multiply (0 = plain) */
+    int split_diagonals;
+    long long kernel_launches;
+} caps_counters;
+
+void caps_get_counters(caps_counters *out);
+void caps_reset_counters(void);
+void caps_set_phase_timing(int enable);
+
+/* Batched independent multiplies of uneven sizes in one persistent launch
+ * per phase (plain or split form), replayed from a CUDA graph when the
+ * same batch shape repeats.  Matrices i use A[i], B[i], C[i] (device,
+ * column-major n[i] x n[i]).  No reference counterpart (the reference runs
+ * one multiply per process). */
+caps_status caps_multiply_batched_dev(int count, const double *const *A, const double *const *B,
+                                      double *const *C, const int *n, const caps_options *opt,
+                                      void *stream);
+
+/* Human-readable text of a status. */
+const char *caps_status_string(caps_status s);
+
+/* Text of the most recent CUDA error seen by this thread ("" if none). */
+const char *caps_last_cuda_error(void);
+
+/* Test hook: make the next `count` device allocations fail (host-side fault
+ * injection, no GPU fault).  count <= 0 disables. */
+void caps_debug_fail_allocations(int count);
+
+/* Releases cached workspace and plans. */
+void caps_release_cache(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CAPS_GB300_H */

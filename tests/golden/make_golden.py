@@ -1,0 +1,110 @@
+"""Generates the committed golden fixtures under tests/golden/.
+
+Run in the build container, where the reference sources and its unmodified
+one-rank build (oracle/build_ref.sh -> oracle/_ref/libcapsref.so) exist:
+
+    python tests/golden/make_golden.py [REFERENCE_DIR]
+
+1. ref_tests.npz -- the reference's own integer known-answer tests
+   (tests/test{28,42,56,196,294,392}.{in,correct,params}): A and B as uint8,
+   the SHA-256 of the exact int64 product (checked equal to .correct here),
+   and every valid one-rank (-b, -r) parameter pair from the .params files.
+2. ref_float.npz -- outputs of the reference's own multiply() (numpy's
+   OpenBLAS dgemm at the leaves) on seeded uniform[-1,1) inputs in CAPS
+   layout; the oracle with the same BLAS must reproduce them bit for bit.
+3. ref_layout.npz -- the reference's distributeFrom1Proc applied to the ramp
+   0..n^2-1 (column-major), i.e. the CAPS layout permutation.
+"""
+import ctypes
+import hashlib
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+
+def read_matrix_file(path):
+    with open(path) as f:
+        toks = f.read().split()
+    return toks
+
+
+def ref_tests(refdir):
+    out = {}
+    sizes = [28, 42, 56, 196, 294, 392]
+    for n in sizes:
+        toks = read_matrix_file(os.path.join(refdir, "tests", "test%d.in" % n))
+        assert int(toks[0]) == n
+        vals = np.array([int(float(t)) for t in toks[1:]], dtype=np.int64)
+        A = vals[: n * n].reshape(n, n)
+        B = vals[n * n: 2 * n * n].reshape(n, n)
+        C = np.array([int(float(t)) for t in read_matrix_file(os.path.join(refdir, "tests", "test%d.correct" % n))],
+                     dtype=np.int64).reshape(n, n)
+        assert np.array_equal(A @ B, C), "numpy product differs from test%d.correct" % n
+        params = []
+        with open(os.path.join(refdir, "tests", "test%d.params" % n)) as f:
+            for line in f:
+                m = re.search(r"-n (\d+) .* -b (\d+) -r (\d+)", line)
+                if m and m.group(1) == "1":
+                    params.append((int(m.group(2)), int(m.group(3))))
+        out["A%d" % n] = A.astype(np.uint8)
+        out["B%d" % n] = B.astype(np.uint8)
+        out["C%d_sha256" % n] = np.frombuffer(hashlib.sha256(C.tobytes()).digest(), dtype=np.uint8)
+        out["params%d" % n] = np.array(params, dtype=np.int32)
+    np.savez_compressed(os.path.join(HERE, "ref_tests.npz"), **out)
+    print("ref_tests.npz:", sum(len(out["params%d" % n]) for n in sizes), "one-rank parameter lines")
+
+
+class Desc(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_int) for f in ("lda", "nrec", "nproc", "nprocr", "nprocc", "nproc_summa", "bs")]
+
+
+FLOAT_CASES = [(56, 2, 1, "dd", 11), (64, 3, 2, "ddd", 12), (96, 1, 4, None, 13), (128, 2, 1, "dd", 14)]
+
+
+def ref_float(reflib):
+    L = ctypes.CDLL(reflib)
+    mul = getattr(L, "_Z8multiplyPdS_S_13MatDescriptorPc")
+    dp = ctypes.POINTER(ctypes.c_double)
+    mul.argtypes = [dp, dp, dp, Desc, ctypes.c_char_p]
+    mul.restype = None
+    out = {}
+    for n, r, bs, pat, seed in FLOAT_CASES:
+        rng = np.random.default_rng(seed)
+        A = rng.uniform(-1, 1, n * n)
+        B = rng.uniform(-1, 1, n * n)
+        C = np.zeros(n * n)
+        mul(A.ctypes.data_as(dp), B.ctypes.data_as(dp), C.ctypes.data_as(dp), Desc(n, r, 1, 1, 1, 1, bs),
+            pat.encode() if pat else None)
+        out["C_%d_%d_%d" % (n, r, bs)] = C
+    np.savez_compressed(os.path.join(HERE, "ref_float.npz"), **out)
+    print("ref_float.npz:", list(out))
+
+
+def ref_layout(reflib):
+    L = ctypes.CDLL(reflib)
+    dist = getattr(L, "_Z19distributeFrom1Proc13MatDescriptorPdS0_")
+    dp = ctypes.POINTER(ctypes.c_double)
+    dist.argtypes = [Desc, dp, dp]
+    dist.restype = None
+    out = {}
+    for n, r, bs in [(56, 2, 7), (56, 3, 1), (48, 2, 4), (28, 0, 4), (64, 3, 2)]:
+        I = np.arange(n * n, dtype=np.float64)
+        O = np.zeros(n * n)
+        dist(Desc(n, r, 1, 1, 1, 1, bs), O.ctypes.data_as(dp), I.ctypes.data_as(dp))
+        out["perm_%d_%d_%d" % (n, r, bs)] = O.astype(np.int32)
+    np.savez_compressed(os.path.join(HERE, "ref_layout.npz"), **out)
+    print("ref_layout.npz:", list(out))
+
+
+if __name__ == "__main__":
+    refdir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    reflib = os.path.join(ROOT, "oracle", "_ref", "libcapsref.so")
+    ref_tests(refdir)
+    ref_float(reflib)
+    ref_layout(reflib)

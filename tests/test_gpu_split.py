@@ -1,0 +1,113 @@
+"""GPU parity of the split (Ozaki-style, tcgen05) form, through the C ABI.
+
+The leaf kernel computes exact integer digit-pair products, so for the same
+digit count s and diagonal count nd it must equal the oracle's CPU model of
+the split arithmetic BIT FOR BIT.  Whole multiplies are bit-exact on integer
+inputs and, on float inputs, within the plain FP64 path's error."""
+import numpy as np
+import pytest
+
+from helpers import caps_of, mat_of, gpu_multiply, dd_of, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _leaf(caps, cuda, A, B, s=0, nd=0):
+    import torch
+    m = A.shape[0]
+    C = torch.full((m * m,), float("nan"), dtype=torch.float64, device=cuda)
+    caps.leaf_gemm(torch.from_numpy(A.T.copy().reshape(-1)).to(cuda),
+                   torch.from_numpy(B.T.copy().reshape(-1)).to(cuda), C, m, form="split", slices=s, diagonals=nd)
+    torch.cuda.synchronize()
+    return C.cpu().numpy().reshape(m, m).T, caps.counters()
+
+
+@pytest.mark.parametrize("m", [128, 64, 14, 200, 512, 1100])
+def test_split_leaf_bitexact_vs_model_uniform(caps, oracle_mod, cuda, m):
+    rng = np.random.default_rng(m)
+    A = rng.uniform(-1, 1, (m, m))
+    B = rng.uniform(-1, 1, (m, m))
+    C, cnt = _leaf(caps, cuda, A, B)
+    s, nd = cnt["split_slices"], cnt["split_diagonals"]
+    assert (s, nd) == (8, 8)
+    ref = oracle_mod.split_gemm(A.T.copy().reshape(-1), B.T.copy().reshape(-1), m, s, nd).reshape(m, m).T
+    assert np.array_equal(C, ref)
+
+
+@pytest.mark.parametrize("s,nd", [(7, 7), (6, 8), (3, 5), (8, 6), (1, 1)])
+def test_split_leaf_bitexact_forced_digits(caps, oracle_mod, cuda, s, nd):
+    m = 192
+    rng = np.random.default_rng(s * 10 + nd)
+    A = rng.uniform(-1, 1, (m, m)) * 2.0 ** rng.integers(-20, 21, (m, m))
+    B = rng.uniform(-1, 1, (m, m))
+    C, cnt = _leaf(caps, cuda, A, B, s, nd)
+    assert (cnt["split_slices"], cnt["split_diagonals"]) == (s, nd)
+    ref = oracle_mod.split_gemm(A.T.copy().reshape(-1), B.T.copy().reshape(-1), m, s, nd).reshape(m, m).T
+    assert np.array_equal(C, ref)
+
+
+@pytest.mark.parametrize("m,lim", [(256, 1024), (640, 9), (2048, 1024)])
+def test_split_leaf_integers_exact(caps, oracle_mod, cuda, m, lim):
+    rng = np.random.default_rng(m)
+    A = rng.integers(-lim, lim + 1, (m, m)).astype(np.float64)
+    B = rng.integers(-lim, lim + 1, (m, m)).astype(np.float64)
+    C, cnt = _leaf(caps, cuda, A, B)
+    assert cnt["split_slices"] <= 4
+    assert np.array_equal(C, (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64))
+
+
+def test_split_leaf_zero_rows_and_tiny_values(caps, oracle_mod, cuda):
+    m = 130
+    rng = np.random.default_rng(9)
+    A = rng.uniform(-1, 1, (m, m))
+    A[3, :] = 0.0
+    A[:, 5] = 0.0
+    A[7, 11] = 1e-300
+    B = rng.uniform(-1, 1, (m, m)) * 1e-200
+    B[:, 2] = 0.0
+    C, cnt = _leaf(caps, cuda, A, B)
+    ref = oracle_mod.split_gemm(A.T.copy().reshape(-1), B.T.copy().reshape(-1), m, cnt["split_slices"],
+                                cnt["split_diagonals"]).reshape(m, m).T
+    assert np.array_equal(C, ref)
+    assert np.all(C[3, :] == 0) and np.all(C[:, 2] == 0)
+
+
+@pytest.mark.parametrize("n", [28, 56, 196, 392])
+def test_reference_known_answers_split(caps, oracle_mod, ref_tests, cuda, n):
+    A = ref_tests["A%d" % n].astype(np.float64)
+    B = ref_tests["B%d" % n].astype(np.float64)
+    exact = (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64)
+    for bs, r in ref_tests["params%d" % n]:
+        for pat in ("d" * r, "b" * r):
+            C = gpu_multiply(caps, oracle_mod, A, B, r, bs, pat, form="split")
+            assert np.array_equal(C, exact), (n, bs, r, pat)
+
+
+def test_config5_like_integers_bitexact(caps, oracle_mod, cuda):
+    """Integers in [-1024, 1024], 'bbdd' (scaled down from n = 32768)."""
+    n, r = 2048, 4
+    rng = np.random.default_rng(5)
+    A = rng.integers(-1024, 1025, (n, n)).astype(np.float64)
+    B = rng.integers(-1024, 1025, (n, n)).astype(np.float64)
+    exact = (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64)
+    for form in ("split", "plain"):
+        C = gpu_multiply(caps, oracle_mod, A, B, r, 1, "bbdd", form=form)
+        assert np.array_equal(C, exact), form
+
+
+@pytest.mark.parametrize("wide", [False, True])
+def test_split_error_no_worse_than_plain(caps, oracle_mod, cuda, wide):
+    n, r = 1024, 3
+    rng = np.random.default_rng(33 + wide)
+    A = rng.uniform(-1, 1, (n, n))
+    B = rng.uniform(-1, 1, (n, n))
+    if wide:
+        A *= 2.0 ** rng.integers(-20, 21, (n, n))
+        B *= 2.0 ** rng.integers(-20, 21, (n, n))
+    hi, lo = dd_of(oracle_mod, A, B)
+    Cp = gpu_multiply(caps, oracle_mod, A, B, r, 1, "ddb", form="plain")
+    Cs = gpu_multiply(caps, oracle_mod, A, B, r, 1, "ddb", form="split")
+    ew_p, nw_p = rel_err(Cp, hi, lo, A, B)
+    ew_s, nw_s = rel_err(Cs, hi, lo, A, B)
+    assert nw_s <= 1.25 * nw_p, (nw_s, nw_p)
+    assert ew_s <= 1.25 * ew_p or ew_s < 1e-13, (ew_s, ew_p)

@@ -1,0 +1,99 @@
+"""CPU tests of the product library: it loads, exports every declared symbol,
+and its host-side logic (validation, pattern choice, workspace sizing, error
+codes) behaves like the reference's entry points.  No kernel runs here."""
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions(path):
+    txt = open(path).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(caps_[a-z_0-9]+)\s*\(", txt)))
+
+
+def test_c_abi_exports_every_declared_symbol(caps):
+    declared = header_functions(os.path.join(ROOT, "include", "caps_gb300.h"))
+    assert set(caps.C_ABI_SYMBOLS) == set(declared)
+    L = caps.lib()
+    for name in declared:
+        assert hasattr(L, name), name
+
+
+def test_compat_header_symbols_exported(caps):
+    out = subprocess.run(["nm", "-D", "--defined-only", caps.LIB_PATH], stdout=subprocess.PIPE, text=True).stdout
+    for mangled in ["_Z8multiplyPdS_S_13MatDescriptorPc", "_Z8allocatex", "_Z10deallocatePdx",
+                    "_Z18setAvailableMemoryx", "_Z12enoughMemoryx", "_Z16getMaxUsedMemoryv",
+                    "_Z17numEntriesPerProc13MatDescriptor", "_Z19distributeFrom1Proc13MatDescriptorPdS0_",
+                    "_Z14collectTo1Proc13MatDescriptorPdS0_", "_Z10initTimersv", "_Z13printCountersd13MatDescriptor",
+                    "_Z17initCommunicationPiPPPci", "_Z20initCommunicationAltPiPPPci", "_Z7getRankv",
+                    "_Z13getLog7nProcsv", "_Z10getPFactorv", "_Z10read_timerv", "_Z7getCommv",
+                    "caps_compat_set_form"]:
+        assert mangled in out, mangled
+    for name in header_functions(os.path.join(ROOT, "include", "caps_compat.h")):
+        assert name in out, name
+
+
+def test_status_strings_and_validation(caps):
+    L = caps.lib()
+    assert L.caps_status_string(1).decode() == "Invalid pattern"
+    d = caps.MatDescriptor.make(56, 2)
+    assert caps.resolve_pattern(d, "db") == "db"
+    with pytest.raises(caps.CapsError) as e:
+        caps.resolve_pattern(d, "dx")
+    assert str(e.value) == "Invalid pattern" and e.value.status == 1
+    with pytest.raises(caps.CapsError) as e:
+        caps.resolve_pattern(d, "d")          # shorter than nrec
+    assert e.value.status == 1
+    with pytest.raises(caps.CapsError) as e:
+        caps.resolve_pattern(caps.MatDescriptor.make(54, 2))  # 54 % 4 != 0
+    assert e.value.status == 2
+    with pytest.raises(caps.CapsError) as e:
+        caps.resolve_pattern(caps.MatDescriptor(56, 2, 7, 7, 1, 1, 1))  # multi-rank descriptor
+    assert e.value.status == 7
+    with pytest.raises(caps.CapsError) as e:
+        caps.workspace_size(caps.MatDescriptor.make(56, 2), "dd", form=3)
+    assert e.value.status == 8
+
+
+def test_workspace_and_auto_pattern(caps):
+    d = caps.MatDescriptor.make(16384, 3)
+    q = (8192 ** 2) * 8
+    ws_ddd = caps.workspace_size(d, "ddd")
+    # 'd' level keeps 11 quarter buffers: 11 q (n/2) + 11 q/4 + 11 q/16
+    assert ws_ddd >= 11 * q * (1 + 1 / 4 + 1 / 16) * 0.99
+    ws_bbb = caps.workspace_size(d, "bbb")
+    assert ws_bbb > ws_ddd
+    # a small budget forces 'd' everywhere, a large one allows 'b' at the bottom
+    assert caps.resolve_pattern(d, None, workspace_limit=1 << 20) == "ddd"
+    p = caps.resolve_pattern(d, None, workspace_limit=64 << 30)
+    assert p.endswith("b")
+    assert caps.workspace_size(d, None, workspace_limit=64 << 30) <= 64 << 30
+    # 'h' behaves as 'd' on one GPU
+    assert caps.workspace_size(d, "hhh") == ws_ddd
+
+
+def test_split_workspace_bounded(caps):
+    d = caps.MatDescriptor.make(16384, 3)
+    ws = caps.workspace_size(d, "bbb", form="split")
+    assert ws < 80 << 30
+
+
+@pytest.mark.skipif(not os.path.isfile("/root/reference/randombenchmark.cpp"), reason="reference sources absent")
+def test_reference_drivers_link_unmodified_against_library(caps, tmp_path):
+    """The reference's own randombenchmark.cpp / fromfile1.cpp compile against
+    the reference headers and link against libcaps_gb300.so alone (no
+    multiply.o / communication.o / memory.o / counters.o / matrix.o / library.o)."""
+    shim = os.path.join(ROOT, "oracle", "ref_shim", "mpi.h")
+    libdir = os.path.dirname(caps.LIB_PATH)
+    for drv in ("randombenchmark", "fromfile1"):
+        out = tmp_path / drv
+        cmd = ["g++", "-O1", "-w", "-include", shim, "-I" + os.path.dirname(shim), "-I/root/reference",
+               "-DNUM_THREADS=1", "/root/reference/%s.cpp" % drv, "-o", str(out), "-L" + libdir, "-lcaps_gb300",
+               "-Wl,-rpath," + libdir]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        assert r.returncode == 0, r.stdout
