@@ -1,0 +1,394 @@
+#!/usr/bin/env python3
+"""Benchmark of the CAPS Strassen multiply on GB300 (one JSON line on rank 0).
+
+Metric: effective TFLOP/s (2 n^3 / t) of the split-digit Strassen multiply at
+n = 16384, r = 3 (uniform[-1,1) float64 inputs, seeded), with the plain FP64
+(DMMA) Strassen of the same multiply timed beside it and the error of both
+measured on sampled entries against a binary128 (numpy longdouble on aarch64)
+classical product.
+
+  value     device-resident: A, B, C already in HBM, K multiplies timed with
+            CUDA events on the launching stream (each matrix is 2 GiB, far
+            above the 129 MB L2, so nothing is served from L2 across steps)
+  e2e       the same through the host entry point: pinned host A, B copied in,
+            C copied out, inside the timed region
+  roofline  the dominant kernel (split_gemm_kernel): digit-pair tensor flops
+            per launch / its average launch time (CUDA events, same stream)
+  cpu_baseline  the oracle restatement of the reference's CPU path (OpenMP +
+            OpenBLAS dgemm) on a bounded sample of the same workload
+
+--impl reference times the reference's CPU path alone (the oracle port on the
+host cores), as the reference arm.  N > 1 GPUs (torchrun) run independent
+replicas: the multiply does not shard across GPUs on this path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+os.environ.setdefault("OMP_WAIT_POLICY", "passive")  # before any OpenMP runtime starts
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "effective TFLOP/s (2n³/t) at n=16384: split-INT8 vs FP64 Strassen, same error"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=16384)
+    ap.add_argument("--nrec", type=int, default=3)
+    ap.add_argument("--pattern", default=None, help="default: the library's choice")
+    ap.add_argument("--slices", type=int, default=0)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--samples", type=int, default=256, help="entries checked against binary128")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join("/tmp", "caps_clocks_%d_%d.csv" % (os.getpid(), index))
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 8:
+                    continue
+                try:
+                    sm.append(float(parts[0]))
+                    mx.append(float(parts[1]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[4:8]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        except OSError:
+            return None
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- peaks
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return d, "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def profiled_traffic():
+    """dram bytes per split_gemm launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "split_gemm_kernel_n16384.md")
+    try:
+        for line in open(p):
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+# ----------------------------------------------------------------- error
+def sampled_error(C_cm, A_cm, B_cm, n, samples, seed=7):
+    """Max elementwise |C - C_ref| / (|A||B|) and normwise over sampled entries;
+    C_ref from binary128 (numpy longdouble) dot products."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    rows = rng.integers(0, n, samples)
+    cols = rng.integers(0, n, samples)
+    ld = np.longdouble
+    Am, Bm, Cm = A_cm.reshape(n, n), B_cm.reshape(n, n), C_cm.reshape(n, n)  # [col][row]
+    ew, num, den = 0.0, 0.0, 0.0
+    for i, j in zip(rows, cols):
+        a = np.ascontiguousarray(Am[:, i])  # row i of A
+        b = Bm[j]                           # column j of B
+        ref = np.dot(a.astype(ld), b.astype(ld))
+        ab = float(np.dot(np.abs(a), np.abs(b)))
+        c = Cm[j, i]
+        d = float(ld(c) - ref)
+        ew = max(ew, abs(d) / ab if ab > 0 else abs(d))
+        num += d * d
+        den += float(ref) ** 2
+    return {"max_elementwise_rel": ew, "normwise_rel": (num / den) ** 0.5 if den > 0 else 0.0,
+            "samples": int(samples), "reference_precision_bits": int(np.finfo(ld).nmant + 1)}
+
+
+# ----------------------------------------------------------------- CPU leg
+def cpu_sample(n, nrec, seed=11):
+    """Oracle port of the reference CPU path on a bounded sample of the
+    workload: the top level's sums and C combination in full plus one of its
+    seven subproducts (n/2, nrec-1) in full; t_full ~ t_top + 7 t_sub."""
+    import numpy as np
+    from oracle import oracle
+    cores = os.cpu_count() or 1
+    oracle.build()
+    blas = oracle.use_blas(True, threads=cores)
+    oracle.set_threads(cores)
+    rng = np.random.default_rng(seed)
+    A = rng.uniform(-1, 1, n * n)
+    B = rng.uniform(-1, 1, n * n)
+    C = np.empty(n * n)
+    t_top, t_sub = oracle.multiply_sample(A, B, C, n, nrec, 1, "d" * nrec, child=1)
+    t_full = t_top + 7 * t_sub
+    del A, B, C
+    return {"t_top": t_top, "t_sub": t_sub, "t_est": t_full, "cores": cores, "blas": blas}
+
+
+def cpu_baseline_entry(n, nrec, s):
+    return {"value": 2.0 * n ** 3 / s["t_est"] / 1e12, "unit": "TFLOP/s", "cores": s["cores"], "kind": "port",
+            "sample": "oracle restatement of the reference CPU path (OpenMP sums, OpenBLAS dgemm leaves, "
+                      "OMP_WAIT_POLICY=passive, %d threads): n=%d r=%d 'd'*r, top-level sums and C combination "
+                      "timed in full (%.2f s) plus 1 of the 7 top-level subproducts (n=%d, r=%d) timed in full "
+                      "(%.2f s); value = 2n^3 / (t_top + 7 t_sub)" % (s["cores"], n, nrec, s["t_top"], n // 2,
+                                                                     nrec - 1, s["t_sub"])}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    n, r = args.n, args.nrec
+    times = []
+    for k in range(args.warmup + args.steps):
+        s = cpu_sample(n, r, seed=11 + k)
+        if k >= args.warmup:
+            times.append(s)
+    t = sum(x["t_est"] for x in times) / len(times)
+    val = 2.0 * n ** 3 / t / 1e12
+    cb = cpu_baseline_entry(n, r, {**times[-1], "t_est": t})
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "TFLOP/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "CAPS Strassen multiply n=%d r=%d, reference CPU path (one rank)" % (n, r),
+                   "n": n, "nrec": r, "pattern": "d" * r, "inputs": "uniform[-1,1) seeded"},
+        "cpu_baseline": cb,
+        "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+# ----------------------------------------------------------------- GPU legs
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    import numpy as np
+    import torch
+    from caps_gb300 import build as cbuild
+    if not os.path.exists(cbuild.LIB):
+        cbuild.build()
+    import caps_gb300 as cg
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n, r = args.n, args.nrec
+    desc = cg.MatDescriptor.make(n, r)
+    pattern = args.pattern or cg.resolve_pattern(desc, None, form="split", workspace_limit=96 << 30)
+    g = torch.Generator(device=dev)
+    g.manual_seed(1234 + rank)
+    A = torch.rand(n * n, dtype=torch.float64, device=dev, generator=g) * 2 - 1
+    B = torch.rand(n * n, dtype=torch.float64, device=dev, generator=g) * 2 - 1
+    C = torch.empty_like(A)
+    stream = torch.cuda.current_stream(dev)
+
+    def step(form, c=C):
+        cg.multiply(A, B, c, desc, pattern, form=form, slices=args.slices, stream=stream.cuda_stream)
+
+    # ---- headline: split form, device resident
+    for _ in range(max(args.warmup, 3)):
+        step("split")
+    torch.cuda.synchronize()
+    cg.set_phase_timing(True)
+    gemm_t, gemm_launches, gemm_m3, launches = 0.0, 0, 0.0, 0
+    barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step("split")
+            c = cg.counters()
+            gemm_t += c["time_leaf_gemm"]
+            gemm_launches += c["leaf_gemm_launches"]
+            gemm_m3 += c["leaf_gemm_m3"]
+            launches += c["kernel_launches"]
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    cg.set_phase_timing(False)
+    t_split = max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps, world)
+    cnt = cg.counters()
+    s_used, nd_used = cnt["split_slices"], cnt["split_diagonals"]
+    value = world * 2.0 * n ** 3 / t_split / 1e12
+
+    # ---- plain FP64 Strassen of the same multiply, and the errors of both
+    out = {}
+    if rank == 0:
+        def colmajor(x):
+            y = torch.empty_like(x)
+            cg.from_caps_layout(x, y, desc)
+            torch.cuda.synchronize()
+            return y.cpu().numpy()
+        A_cm, B_cm = colmajor(A), colmajor(B)
+        err_split = sampled_error(colmajor(C), A_cm, B_cm, n, args.samples)
+        plain = None
+        if not args.no_plain:
+            Cp = torch.empty_like(A)
+            step("plain", Cp)
+            torch.cuda.synchronize()
+            p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            p0.record(stream)
+            step("plain", Cp)
+            p1.record(stream)
+            torch.cuda.synchronize()
+            t_plain = p0.elapsed_time(p1) / 1e3
+            err_plain = sampled_error(colmajor(Cp), A_cm, B_cm, n, args.samples)
+            plain = {"value": 2.0 * n ** 3 / t_plain / 1e12, "ms_per_step": t_plain * 1e3, "steps": 1,
+                     "error": err_plain, "pattern": pattern}
+            del Cp
+        out["split_error"] = err_split
+        out["plain"] = plain
+        del A_cm, B_cm
+
+    # ---- e2e through the host entry point (pinned host buffers)
+    hA = torch.empty(n * n, dtype=torch.float64, pin_memory=True)
+    hB = torch.empty(n * n, dtype=torch.float64, pin_memory=True)
+    hC = torch.empty(n * n, dtype=torch.float64, pin_memory=True)
+    hA.copy_(A)
+    hB.copy_(B)
+    del A, B, C
+    torch.cuda.empty_cache()
+    nA, nB, nC = hA.numpy(), hB.numpy(), hC.numpy()
+    cg.multiply(nA, nB, nC, desc, pattern, form="split", slices=args.slices)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cg.multiply(nA, nB, nC, desc, pattern, form="split", slices=args.slices)
+    t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
+    barrier(world)
+
+    if rank == 0:
+        peaks, peak_src = measured_peaks()
+        pairs = cg.digit_pairs(s_used, nd_used)
+        per_launch_flops = 2.0 * pairs * gemm_m3 / max(gemm_launches, 1)
+        per_launch_s = gemm_t / max(gemm_launches, 1)
+        achieved = per_launch_flops / per_launch_s / 1e12 if per_launch_s > 0 else 0.0
+        peak = float(peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops", 1700.0)))
+        traffic = profiled_traffic()
+        cpu = None
+        if not args.no_cpu:
+            try:
+                cpu = cpu_baseline_entry(n, r, cpu_sample(n, r))
+            except Exception as ex:  # the baseline is reported, never required
+                cpu = {"value": None, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
+                       "sample": "failed: %s" % ex}
+        plain = out.get("plain")
+        line = {
+            "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_split * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "CAPS Strassen multiply C=A*B, n=%d, r=%d, split-digit base case" % (n, r),
+                       "n": n, "nrec": r, "pattern": pattern, "form": "split", "slices": s_used,
+                       "diagonals": nd_used, "digit_pairs": pairs,
+                       "inputs": "float64 uniform[-1,1) seeded (torch.Generator), CAPS layout",
+                       "l2": "inputs larger than L2 (each matrix 2 GiB vs 129 MB L2)",
+                       "parallelism": "replicas x%d" % world},
+            "split_vs_plain": (value / world) / plain["value"] if plain else None,
+            "plain_fp64": plain,
+            "error": {"split": out.get("split_error"), "plain": plain["error"] if plain else None,
+                      "definition": "max over sampled (i,j) of |C_ij - C_ref_ij| / (|A||B|)_ij, and "
+                                    "||C - C_ref||_2 / ||C_ref||_2 over the same entries; C_ref = binary128 dot"},
+            "roofline": {"bound": "tensor", "kernel": "split_gemm_kernel", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "traffic": traffic,
+                         "peak_source": "%s bf16_tflops_sustained (of %s)" % (peak_src, peak_src),
+                         "flops_per_launch": per_launch_flops, "launches": gemm_launches,
+                         "avg_launch_ms": per_launch_s * 1e3,
+                         "unit_of_work": "digit-pair products: %d pairs x 2 m^3 per leaf" % pairs},
+            "cpu_baseline": cpu,
+            "e2e": {"value": world * 2.0 * n ** 3 / t_e2e / 1e12, "unit": "TFLOP/s",
+                    "h2d_bytes_per_step": 2 * n * n * 8, "d2h_bytes_per_step": n * n * 8,
+                    "ms_per_step": t_e2e * 1e3, "api": "caps_multiply_host (pinned host buffers)"},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

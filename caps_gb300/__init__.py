@@ -74,7 +74,8 @@ class Counters(ctypes.Structure):
                 ("time_add", ctypes.c_double), ("time_mul", ctypes.c_double),
                 ("time_rearrange", ctypes.c_double), ("workspace_peak_bytes", ctypes.c_longlong),
                 ("split_slices", ctypes.c_int), ("split_diagonals", ctypes.c_int),
-                ("kernel_launches", ctypes.c_longlong)]
+                ("kernel_launches", ctypes.c_longlong), ("time_leaf_gemm", ctypes.c_double),
+                ("leaf_gemm_launches", ctypes.c_longlong), ("leaf_gemm_m3", ctypes.c_double)]
 
 
 _lib = None
@@ -266,6 +267,11 @@ def debug_fail_allocations(count: int) -> None:
 class Flops:
     effective: float  # 2 n^3
     actual: float     # additions + multiplications as counters.cpp counts them
+
+
+def digit_pairs(s: int, nd: int) -> int:
+    """Digit-pair products of the split form: pairs (a, b), 1 <= a, b <= s, a + b <= nd + 1."""
+    return sum(1 for a in range(1, s + 1) for b in range(1, s + 1) if a + b <= nd + 1)
 
 
 def flop_counts(n: int, nrec: int) -> Flops:

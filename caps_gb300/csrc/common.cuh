@@ -95,6 +95,10 @@ cudaError_t launch_split_scan(const LeafTask *tasks_dev, int count, int m, void 
                              cudaStream_t stream);
 // Reads back the digits needed (max over the batch) from the scan results.
 cudaError_t split_needed_slices(void *workspace, int count, int m, int *needed, cudaStream_t stream);
+// f / g exponents, digit count, and the digit planes (finalize + slice).
+cudaError_t launch_split_prep(const LeafTask *tasks_dev, int count, int m, SplitParams p,
+                              void *workspace, cudaStream_t stream);
+// The tcgen05 digit-pair GEMM with the exact recombination epilogue.
 cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, SplitParams p,
                               void *workspace, unsigned int *status_dev, cudaStream_t stream);
 

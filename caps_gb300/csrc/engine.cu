@@ -461,7 +461,13 @@ static caps_status plan(const double *A, const double *B, double *C, const caps_
 }
 
 // ------------------------------------------------------------------ run
-static caps_status run_ops(Planned &pl, cudaStream_t s, double *phase_time) {
+struct KernelTiming {
+    double gemm_seconds = 0;   // base-case GEMM kernels only (DMMA or tcgen05)
+    long long gemm_launches = 0;
+    double gemm_leaf_m3 = 0;   // sum over launches of count * m^3
+};
+
+static caps_status run_ops(Planned &pl, cudaStream_t s, double *phase_time, KernelTiming *kt) {
     char *tables = g_arena.ptr + pl.table_off;
     if (!pl.b.blob.empty()) {
         CAPS_TRY(pinned_reserve(pl.b.blob.size()));
@@ -470,61 +476,86 @@ static caps_status run_ops(Planned &pl, cudaStream_t s, double *phase_time) {
         CAPS_CUDA_TRY(cudaEventRecord(g_pinned.done, s));
         g_pinned.pending = true;
     }
-    std::vector<cudaEvent_t> ev;
-    std::vector<int> evphase;
+    struct Rec {
+        cudaEvent_t e0, e1;
+        int phase;
+        bool gemm;
+        double m3;
+    };
+    std::vector<Rec> recs;
+    auto ev_begin = [&](cudaEvent_t &e) {
+        cudaEventCreate(&e);
+        cudaEventRecord(e, s);
+    };
     for (const Op &o : pl.b.ops) {
-        cudaEvent_t e0 = nullptr, e1 = nullptr;
-        if (phase_time) {
-            cudaEventCreate(&e0);
-            cudaEventCreate(&e1);
-            cudaEventRecord(e0, s);
-        }
+        const bool timed = phase_time || kt;
+        Rec r{nullptr, nullptr, PH_ADD, false, 0.0};
         cudaError_t err = cudaSuccess;
-        int ph = PH_ADD;
         switch (o.kind) {
             case K_EW:
+                if (timed) ev_begin(r.e0);
                 err = launch_elementwise(o.ew, reinterpret_cast<const EwTask *>(tables + o.toff), o.count, o.q, s, o.vec);
-                ph = PH_ADD;
+                r.phase = PH_ADD;
                 break;
             case K_LEAF_DMMA:
+                if (timed) ev_begin(r.e0);
                 err = launch_dmma_gemm(reinterpret_cast<const LeafTask *>(tables + o.toff), o.count, o.m, s);
-                ph = PH_MUL;
+                r.phase = PH_MUL;
+                r.gemm = true;
+                r.m3 = (double)o.count * o.m * (double)o.m * o.m;
                 break;
             case K_LEAF_SPLIT: {
                 const LeafTask *t = reinterpret_cast<const LeafTask *>(tables + o.toff);
                 void *ws = g_arena.ptr + o.split_off;
+                // scan + prep are timed with the multiply phase but not as GEMM
+                Rec pre{nullptr, nullptr, PH_MUL, false, 0.0};
+                if (timed) ev_begin(pre.e0);
                 err = launch_split_scan(t, o.count, o.m, ws, s);
-                if (err == cudaSuccess)
-                    err = launch_split_gemm(t, o.count, o.m, o.sp, ws, reinterpret_cast<unsigned *>(g_status.ptr), s);
-                ph = PH_MUL;
+                if (err == cudaSuccess) err = launch_split_prep(t, o.count, o.m, o.sp, ws, s);
+                if (timed) {
+                    cudaEventCreate(&pre.e1);
+                    cudaEventRecord(pre.e1, s);
+                    recs.push_back(pre);
+                }
+                if (err != cudaSuccess) break;
+                if (timed) ev_begin(r.e0);
+                err = launch_split_gemm(t, o.count, o.m, o.sp, ws, reinterpret_cast<unsigned *>(g_status.ptr), s);
+                r.phase = PH_MUL;
+                r.gemm = true;
+                r.m3 = (double)o.count * o.m * (double)o.m * o.m;
                 break;
             }
             case K_REORDER_LEAF:
+                if (timed) ev_begin(r.e0);
                 err = launch_reorder(reinterpret_cast<const double *const *>(tables + o.toff),
                                      reinterpret_cast<double *const *>(tables + o.toff2), o.count, o.m, 0,
                                      o.bs, o.to_caps, s);
-                ph = PH_REARRANGE;
+                r.phase = PH_REARRANGE;
                 break;
         }
         if (err != cudaSuccess) {
             note_cuda_error(err, "kernel launch");
             return CAPS_ERR_CUDA;
         }
-        if (phase_time) {
-            cudaEventRecord(e1, s);
-            ev.push_back(e0);
-            ev.push_back(e1);
-            evphase.push_back(ph);
+        if (timed) {
+            cudaEventCreate(&r.e1);
+            cudaEventRecord(r.e1, s);
+            recs.push_back(r);
         }
     }
-    if (phase_time) {
+    if (!recs.empty()) {
         CAPS_CUDA_TRY(cudaStreamSynchronize(s));
-        for (size_t i = 0; i < evphase.size(); i++) {
+        for (Rec &r : recs) {
             float ms = 0;
-            cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]);
-            phase_time[evphase[i]] += ms * 1e-3;
-            cudaEventDestroy(ev[2 * i]);
-            cudaEventDestroy(ev[2 * i + 1]);
+            cudaEventElapsedTime(&ms, r.e0, r.e1);
+            if (phase_time) phase_time[r.phase] += ms * 1e-3;
+            if (kt && r.gemm) {
+                kt->gemm_seconds += ms * 1e-3;
+                kt->gemm_launches += 1;
+                kt->gemm_leaf_m3 += r.m3;
+            }
+            cudaEventDestroy(r.e0);
+            cudaEventDestroy(r.e1);
         }
     }
     return CAPS_OK;
@@ -585,7 +616,11 @@ static caps_status multiply_dev_locked(const double *A, const double *B, double 
     CAPS_TRY(plan(A, B, C, d, pat, o, g_arena.ptr, pl));
     double pt[3] = {0, 0, 0};
     long long l0 = g_launches;
-    CAPS_TRY(run_ops(pl, s, g_phase_timing ? pt : nullptr));
+    KernelTiming kt;
+    CAPS_TRY(run_ops(pl, s, g_phase_timing ? pt : nullptr, g_phase_timing ? &kt : nullptr));
+    g_counters.time_leaf_gemm = kt.gemm_seconds;
+    g_counters.leaf_gemm_launches = kt.gemm_launches;
+    g_counters.leaf_gemm_m3 = kt.gemm_leaf_m3;
     g_counters.additions = pl.b.adds;
     g_counters.multiplications = pl.b.muls;
     g_counters.time_add = pt[PH_ADD];

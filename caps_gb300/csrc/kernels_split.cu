@@ -227,9 +227,42 @@ __global__ void __launch_bounds__(256) split_finalize_kernel(char *__restrict__ 
 }
 
 // ---------------------------------------------------------------- slice
+// round(x 2^f) to nearest, ties to even, for |x 2^f| <= 2^55, by integer
+// operations on the IEEE bits (the FP64 pipe runs at 1/64 of FP32 here).
+// With x = +-M 2^e (M < 2^53) and f = 55 - E, E >= e + 53, the shift e + f
+// is at most 3, so a left shift never overflows.
+__device__ __forceinline__ long long scaled_round(double x, int f) {
+    unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    int field = (int)((u >> 52) & 0x7ff);
+    unsigned long long M = u & 0xFFFFFFFFFFFFFull;
+    int e;
+    if (field == 0) {
+        if (M == 0) return 0;
+        e = -1074;
+    } else {
+        M |= 1ull << 52;
+        e = field - 1075;
+    }
+    int sh = e + f;
+    unsigned long long q;
+    if (sh >= 0) {
+        q = M << sh;
+    } else {
+        int r = -sh;
+        if (r > 63) {
+            q = 0;
+        } else {
+            q = M >> r;
+            unsigned long long rem = M & ((1ull << r) - 1), half = 1ull << (r - 1);
+            if (rem > half || (rem == half && (q & 1))) q++;
+        }
+    }
+    return (u >> 63) ? -(long long)q : (long long)q;
+}
+
 // balanced base-128 digits of round(x 2^f), most significant first
 __device__ __forceinline__ void digits8(double x, int f, int (&d)[8]) {
-    long long R = __double2ll_rn(scalbn(x, f));
+    long long R = scaled_round(x, f);
 #pragma unroll
     for (int k = 7; k >= 0; k--) {
         long long low = R & 127;
@@ -240,10 +273,10 @@ __device__ __forceinline__ void digits8(double x, int f, int (&d)[8]) {
     d[0] += (int)(R * 128);
 }
 
-// |d| <= 64 has at most 7 significant bits, so the top half of its fp32
-// encoding is its exact bf16 encoding
+// |d| <= 64 has at most 7 significant bits: 1.5 * 2^23 + d is exact in fp32,
+// and the top half of the fp32 encoding of d is its exact bf16 encoding
 __device__ __forceinline__ uint32_t bf16_of_digit(int d) {
-    return __float_as_uint(__int2float_rn(d)) >> 16;
+    return __float_as_uint(__int_as_float(0x4B400000 + d) - 12582912.0f) >> 16;
 }
 
 // A side: one thread = one row x 8 k (16 bytes per plane); 256 threads = one
@@ -423,18 +456,51 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// issues MMAs of A plane a (1-based) against B planes covering diagonal
-// regions [ra, rb] (region r = a + j - 2), four planes per instruction
-__device__ __forceinline__ void issue_range(uint32_t tmem, uint32_t a_base, uint32_t b_base,
-                                            int a, int ra, int rb, uint32_t acc) {
-    for (int r = ra; r <= rb; r += 4) {
-        int cnt = rb - r + 1 < 4 ? rb - r + 1 : 4;
-        int j0 = r - (a - 1) + 1;
-        // K-direction core-matrix stride (LBO) 128 B, M/N-direction (SBO) 256 B
-        uint64_t ad = sdesc(a_base + (uint32_t)(a - 1) * A_PLANE_BYTES, 128, 256);
-        uint64_t bd = sdesc(b_base + (uint32_t)(j0 - 1) * B_PLANE_BYTES, 128, 256);
-        umma(tmem + (uint32_t)(TN * r), ad, bd, idesc_bf16(TM, TN * cnt), acc);
+}  // namespace
+
+namespace {
+
+// The MMA sequence of one 16-deep K step depends only on (s, nd) and on the
+// stage: it is built once per CTA (stage 0 addresses), kept in registers, and
+// each step adds the stage offset to the descriptors' address fields.
+// Recomputing descriptors per MMA in the single issuing thread halved the
+// tensor pipe's throughput.  At most 12 MMAs per step for s, nd <= 8.
+constexpr int MAX_MMA = 12;
+
+struct MmaTable {
+    uint64_t ad[MAX_MMA], bd[MAX_MMA];
+    uint32_t id[MAX_MMA], col[MAX_MMA];
+    uint32_t fresh;  // bit q: MMA q is the first writer of its regions in a chunk
+    int count;
+};
+
+__device__ void build_mma_table(MmaTable *t, uint32_t a0, uint32_t b0, int s, int nd) {
+    int q = 0, init_hi = -1;
+    t->fresh = 0;
+    for (int a = 1; a <= s; a++) {
+        int jmax = s < nd + 1 - a ? s : nd + 1 - a;
+        if (jmax < 1) break;
+        int rlo = a - 1, rhi = a - 1 + jmax - 1;
+        for (int part = 0; part < 2; part++) {
+            // part 0: regions already written this chunk (accumulate);
+            // part 1: regions this plane writes first (overwrite on a chunk's first step)
+            int ra = part == 0 ? rlo : (rlo > init_hi + 1 ? rlo : init_hi + 1);
+            int rb = part == 0 ? (rhi < init_hi ? rhi : init_hi) : rhi;
+            for (int r = ra; r <= rb && q < MAX_MMA; r += 4) {
+                int cnt = rb - r + 1 < 4 ? rb - r + 1 : 4;
+                int j0 = r - (a - 1) + 1;
+                // K-direction core-matrix stride (LBO) 128 B, M/N-direction (SBO) 256 B
+                t->ad[q] = sdesc(a0 + (uint32_t)(a - 1) * A_PLANE_BYTES, 128, 256);
+                t->bd[q] = sdesc(b0 + (uint32_t)(j0 - 1) * B_PLANE_BYTES, 128, 256);
+                t->id[q] = idesc_bf16(TM, TN * cnt);
+                t->col[q] = (uint32_t)(TN * r);
+                if (part == 1) t->fresh |= 1u << q;
+                q++;
+            }
+        }
+        if (rhi > init_hi) init_hi = rhi;
     }
+    t->count = q;
 }
 
 }  // namespace
@@ -449,6 +515,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + NSTAGE * STAGE_BYTES);
     // bars: full[NSTAGE], empty[NSTAGE], tfull, tempty, final
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * NSTAGE + 3);
+    MmaTable *mtab = reinterpret_cast<MmaTable *>(bars + 16);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int s, nd;
@@ -521,6 +588,18 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
+            build_mma_table(mtab, smem_u32(stA), smem_u32(stB), s, nd);
+            uint64_t tad[MAX_MMA], tbd[MAX_MMA];
+            uint32_t tid[MAX_MMA], tcol[MAX_MMA];
+#pragma unroll
+            for (int q = 0; q < MAX_MMA; q++) {
+                tad[q] = mtab->ad[q];
+                tbd[q] = mtab->bd[q];
+                tid[q] = mtab->id[q];
+                tcol[q] = tmem + mtab->col[q];
+            }
+            const uint32_t tfresh = mtab->fresh;
+            const int nmma = mtab->count;
             int stage = 0;
             uint32_t phase = 0, chunk_ctr = 0;
             bool ok = true;
@@ -532,19 +611,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                     for (int ks = ks0; ks < ks1; ks++) {
                         if (!mbar_wait(full0 + 8 * stage, phase, status, 8u)) { ok = false; break; }
                         tc_fence_after();
-                        uint32_t a_base = smem_u32(stA + stage * STAGE_A);
-                        uint32_t b_base = smem_u32(stB + stage * STAGE_B);
-                        int init_hi = (ks == ks0) ? -1 : 1000;
-                        for (int a = 1; a <= s; a++) {
-                            int jmax = s < nd + 1 - a ? s : nd + 1 - a;
-                            if (jmax < 1) break;
-                            int rlo = a - 1, rhi = a - 1 + jmax - 1;
-                            int m1 = rhi < init_hi ? rhi : init_hi;
-                            if (rlo <= m1) issue_range(tmem, a_base, b_base, a, rlo, m1, 1u);
-                            int f0 = rlo > init_hi + 1 ? rlo : init_hi + 1;
-                            if (f0 <= rhi) issue_range(tmem, a_base, b_base, a, f0, rhi, 0u);
-                            if (rhi > init_hi) init_hi = rhi;
-                        }
+                        // stage offsets added to the descriptors' address field (>> 4)
+                        const uint64_t soffA = (uint64_t)((uint32_t)(stage * STAGE_A) >> 4);
+                        const uint64_t soffB = (uint64_t)((uint32_t)(stage * STAGE_B) >> 4);
+                        const uint32_t fmask = (ks == ks0) ? tfresh : 0u;
+#pragma unroll
+                        for (int q = 0; q < MAX_MMA; q++)
+                            if (q < nmma) umma(tcol[q], tad[q] + soffA, tbd[q] + soffB, tid[q], ((fmask >> q) & 1u) ^ 1u);
                         umma_commit(empty0 + 8 * stage);
                         if (++stage == NSTAGE) { stage = 0; phase ^= 1; }
                     }
@@ -646,11 +719,10 @@ cudaError_t launch_split_scan(const LeafTask *tasks_dev, int count, int m, void 
     return cudaGetLastError();
 }
 
-cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
-                              unsigned int *status_dev, cudaStream_t stream) {
+cudaError_t launch_split_prep(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
+                              cudaStream_t stream) {
     Geo g = make_geo(m, count);
     char *ws = (char *)workspace;
-    cudaError_t e;
     {
         dim3 grid((unsigned)((m + 255) / 256), (unsigned)count);
         split_finalize_kernel<<<grid, 256, 0, stream>>>(ws, g);
@@ -664,13 +736,21 @@ cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, Split
         split_slice_kernel<<<grid, 256, 0, stream>>>(tasks_dev, m, ws, g, p);
         count_launch();
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
+                              unsigned int *status_dev, cudaStream_t stream) {
+    Geo g = make_geo(m, count);
+    char *ws = (char *)workspace;
+    cudaError_t e;
     if (g_num_sms == 0) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
         if (g_num_sms <= 0) g_num_sms = 152;
     }
-    size_t smem = (size_t)NSTAGE * STAGE_BYTES + 1024 + 256;
+    size_t smem = (size_t)NSTAGE * STAGE_BYTES + 1024 + 1024;
     e = cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int64_t total = (int64_t)g.mtiles * g.ntiles * count;

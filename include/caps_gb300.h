@@ -115,6 +115,9 @@ typedef struct caps_counters {
     int split_slices;        /* digits used by the last split multiply (0 = plain) */
     int split_diagonals;
     long long kernel_launches;
+    double time_leaf_gemm;   /* seconds in base-case GEMM kernels alone (phase timing on) */
+    long long leaf_gemm_launches;
+    double leaf_gemm_m3;     /* sum of leaves * m^3 over those launches */
 } caps_counters;
 
 void caps_get_counters(caps_counters *out);

@@ -149,12 +149,39 @@ static void base_case(int64_t m, int64_t bs, const double *A, const double *B, d
 /* ---------------------------------------------------------------------- */
 static int64_t g_adds = 0, g_muls = 0;
 
+/* Bounded-sample mode for the CPU baseline: at the top level, run every
+ * operand sum and C combination but recurse into only subproduct
+ * g_sample_child (1..7); the seconds spent in sums and in that one
+ * recursion are recorded.  0 = normal operation. */
+static int g_sample_child = 0;
+static double g_sample_t_top = 0.0, g_sample_t_sub = 0.0;
+
+static double now_s(void)
+{
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return 0.0;
+#endif
+}
+
 static void rec(const double *A, const double *B, double *C, int64_t n, int nrec, int64_t bs,
                 const char *pattern);
 
 static void step(const double *A, const double *B, double *C, int64_t n, int nrec, int64_t bs,
                  const char *pattern)
 {
+    const int sample = g_sample_child;
+    g_sample_child = 0; /* only the top level samples */
+    double t_enter = now_s(), t_in_rec = 0.0;
+#define REC(child, a, b, c)                                                   \
+    do {                                                                      \
+        if (!sample || sample == (child)) {                                   \
+            double _t0 = now_s();                                             \
+            rec(a, b, c, h, nrec - 1, bs, pattern);                           \
+            if (sample) { g_sample_t_sub = now_s() - _t0; t_in_rec += g_sample_t_sub; } \
+        }                                                                     \
+    } while (0)
     int64_t h = n / 2, q = h * h;
     const double *A11 = A, *A21 = A + q, *A12 = A + 2 * q, *A22 = A + 3 * q;
     const double *B11 = B, *B21 = B + q, *B12 = B + 2 * q, *B22 = B + 3 * q;
@@ -183,28 +210,30 @@ static void step(const double *A, const double *B, double *C, int64_t n, int nre
      *   U3 = U1+Q3;   C12 = U3+Q6. */
     double *U = (double *)malloc((size_t)(2 * q) * sizeof(double));
     double *U2 = U, *U3 = U + q;
-    rec(A11, B11, C11, h, nrec - 1, bs, pattern);          /* Q1 in C11 */
-    rec(T4, S4, Qt, h, nrec - 1, bs, pattern);              /* Q4 */
+    REC(1, A11, B11, C11);                                  /* Q1 in C11 */
+    REC(4, T4, S4, Qt);                                     /* Q4 */
 #pragma omp parallel for num_threads(g_threads) schedule(static)
     for (int64_t i = 0; i < q; i++) { double u1 = C11[i] + Qt[i]; U2[i] = u1; U3[i] = u1; }
-    rec(T5, S5, Qt, h, nrec - 1, bs, pattern);              /* Q5 */
+    REC(5, T5, S5, Qt);                                     /* Q5 */
 #pragma omp parallel for num_threads(g_threads) schedule(static)
     for (int64_t i = 0; i < q; i++) U2[i] = U2[i] + Qt[i];
-    rec(T3, S3, Qt, h, nrec - 1, bs, pattern);              /* Q3 */
+    REC(3, T3, S3, Qt);                                     /* Q3 */
 #pragma omp parallel for num_threads(g_threads) schedule(static)
     for (int64_t i = 0; i < q; i++) { C22[i] = U2[i] + Qt[i]; U3[i] = U3[i] + Qt[i]; }
-    rec(A22, S7, Qt, h, nrec - 1, bs, pattern);             /* Q7 */
+    REC(7, A22, S7, Qt);                                    /* Q7 */
 #pragma omp parallel for num_threads(g_threads) schedule(static)
     for (int64_t i = 0; i < q; i++) C21[i] = U2[i] - Qt[i];
-    rec(T6, B22, Qt, h, nrec - 1, bs, pattern);             /* Q6 */
+    REC(6, T6, B22, Qt);                                    /* Q6 */
 #pragma omp parallel for num_threads(g_threads) schedule(static)
     for (int64_t i = 0; i < q; i++) C12[i] = U3[i] + Qt[i];
-    rec(A12, B21, Qt, h, nrec - 1, bs, pattern);            /* Q2 */
+    REC(2, A12, B21, Qt);                                   /* Q2 */
 #pragma omp parallel for num_threads(g_threads) schedule(static)
     for (int64_t i = 0; i < q; i++) C11[i] = C11[i] + Qt[i];
     g_adds += 7 * q;
     free(U);
     free(W);
+    if (sample) g_sample_t_top = (now_s() - t_enter) - t_in_rec;
+#undef REC
 }
 
 static int g_bad_pattern = 0;
@@ -240,6 +269,24 @@ int caps_oracle_multiply(const double *A, const double *B, double *C, int64_t n,
     g_bad_pattern = 0;
     rec(A, B, C, n, nrec, bs, pattern);
     return g_bad_pattern ? -1 : 0;
+}
+
+/* Bounded sample of a multiply for the CPU baseline: all top-level sums and
+ * combinations, one of the seven subproducts (child 1..7) in full.  Returns
+ * the seconds in top-level sums and in the subproduct; the full run takes
+ * about t_top + 7 t_sub.  C holds no meaningful result afterwards. */
+int caps_oracle_multiply_sample(const double *A, const double *B, double *C, int64_t n, int nrec,
+                                int64_t bs, const char *pattern, int child, double *t_top,
+                                double *t_sub)
+{
+    if (nrec < 1 || child < 1 || child > 7) return -2;
+    g_sample_child = child;
+    g_sample_t_top = g_sample_t_sub = 0.0;
+    int rc = caps_oracle_multiply(A, B, C, n, nrec, bs, pattern);
+    g_sample_child = 0;
+    *t_top = g_sample_t_top;
+    *t_sub = g_sample_t_sub;
+    return rc;
 }
 
 /* add/multiply counters as the reference counts them (counters.cpp). */

@@ -80,6 +80,9 @@ def lib():
         L.caps_oracle_counters.restype = None
         L.caps_oracle_counters.argtypes = [_i64p, _i64p]
         L.caps_oracle_reset_counters.restype = None
+        L.caps_oracle_multiply_sample.restype = ctypes.c_int
+        L.caps_oracle_multiply_sample.argtypes = [_dp, _dp, _dp, ctypes.c_int64, ctypes.c_int, ctypes.c_int64,
+                                                  ctypes.c_char_p, ctypes.c_int, _dp, _dp]
         L.caps_oracle_set_threads(os.cpu_count() or 1)
         _lib = L
     return _lib
@@ -146,6 +149,18 @@ def multiply(A: np.ndarray, B: np.ndarray, n: int, nrec: int, bs: int = 1,
     if rc == -2:
         raise ValueError("matrix size not divisible by 2^nrec*bs")
     return C
+
+
+def multiply_sample(A: np.ndarray, B: np.ndarray, C: np.ndarray, n: int, nrec: int, bs: int = 1,
+                    pattern: str | None = None, child: int = 1):
+    """Bounded sample of multiply(): (t_top_sums, t_one_subproduct) in seconds."""
+    t_top, t_sub = ctypes.c_double(), ctypes.c_double()
+    pat = pattern.encode() if pattern is not None else None
+    rc = lib().caps_oracle_multiply_sample(_p(A), _p(B), _p(C), n, nrec, bs, pat, child,
+                                           ctypes.byref(t_top), ctypes.byref(t_sub))
+    if rc != 0:
+        raise ValueError("bad sample arguments")
+    return t_top.value, t_sub.value
 
 
 def counters():
