@@ -42,6 +42,7 @@ C_ABI_SYMBOLS = [
     "caps_from_caps_layout_dev", "caps_leaf_gemm_dev", "caps_workspace_size", "caps_resolve_pattern",
     "caps_get_counters", "caps_reset_counters", "caps_set_phase_timing", "caps_multiply_batched_dev",
     "caps_status_string", "caps_last_cuda_error", "caps_debug_fail_allocations", "caps_release_cache",
+    "caps_leaf_gemm_split_noalloc_dev",
 ]
 
 
@@ -124,6 +125,8 @@ def lib() -> ctypes.CDLL:
         L.caps_debug_fail_allocations.restype = None
         L.caps_release_cache.argtypes = []
         L.caps_release_cache.restype = None
+        L.caps_leaf_gemm_split_noalloc_dev.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
+        L.caps_leaf_gemm_split_noalloc_dev.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -197,6 +200,16 @@ def leaf_gemm(A, B, C, m: int, form: int | str = CAPS_FORM_PLAIN, slices: int = 
     opt = options(form, slices, diagonals)
     _check(lib().caps_leaf_gemm_dev(_dev_ptr(A, "A"), _dev_ptr(B, "B"), _dev_ptr(C, "C"), int(m),
                                     ctypes.byref(opt), _stream_ptr(stream)))
+
+
+NOALLOC_MAX_M = 512
+
+
+def leaf_gemm_split_noalloc(A, B, C, m: int, slices: int = 0, diagonals: int = 0, stream=None) -> None:
+    """Split-form base case that allocates nothing (scratch in a static device
+    array; 1 <= m <= 512; synchronises the stream)."""
+    _check(lib().caps_leaf_gemm_split_noalloc_dev(_dev_ptr(A, "A"), _dev_ptr(B, "B"), _dev_ptr(C, "C"), int(m),
+                                                  int(slices), int(diagonals), _stream_ptr(stream)))
 
 
 def to_caps_layout(colmajor, out, desc: MatDescriptor, stream=None) -> None:

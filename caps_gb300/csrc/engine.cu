@@ -40,6 +40,7 @@ static bool g_phase_timing = false;
 void note_cuda_error(cudaError_t e, const char *where) {
     g_last_err = std::string(cudaGetErrorString(e)) + " (" + where + ")";
 }
+void set_last_error_text(const char *msg) { g_last_err = msg; }
 void count_launch(long long n) { g_launches += n; }
 
 static caps_status dev_malloc(void **p, size_t bytes) {

@@ -92,6 +92,22 @@ caps_status caps_from_caps_layout_dev(const double *caps, double *colmajor, caps
 caps_status caps_leaf_gemm_dev(const double *A, const double *B, double *C, int m,
                                const caps_options *opt, void *stream);
 
+/* Split-form base case C = A * B (column-major m x m, device pointers) that
+ * allocates nothing.  No counterpart in the reference.  For callers that
+ * cannot let a library call cudaMalloc -- an application whose device memory
+ * is all handed to its own pool allocator, or a code path that cannot take
+ * the device-wide synchronisation of cudaMalloc / cudaFree.  Its scratch
+ * (digit planes, scales, task table, status word) lives in a file-scope
+ * device array of 8.5 MiB that every GPU loading the library holds until
+ * exit.  Limits: 1 <= m <= 512, otherwise CAPS_ERR_SIZE and nothing runs.
+ * slices / diagonals as in caps_options (0 = automatic).  All calls share
+ * the array, so calls that overlap on the GPU race: serialise them.  The
+ * first call on a device looks up the array's address with that device
+ * current; make it before any stream capture begins.  Synchronises
+ * `stream` before returning (it reads the kernels' status word back). */
+caps_status caps_leaf_gemm_split_noalloc_dev(const double *A, const double *B, double *C, int m,
+                                             int slices, int diagonals, void *stream);
+
 /* Workspace bytes caps_multiply_dev needs for (desc, pattern, opt). */
 caps_status caps_workspace_size(caps_desc desc, const char *pattern, const caps_options *opt,
                                 long long *bytes);
