@@ -42,7 +42,7 @@ C_ABI_SYMBOLS = [
     "caps_from_caps_layout_dev", "caps_leaf_gemm_dev", "caps_workspace_size", "caps_resolve_pattern",
     "caps_get_counters", "caps_reset_counters", "caps_set_phase_timing", "caps_multiply_batched_dev",
     "caps_status_string", "caps_last_cuda_error", "caps_debug_fail_allocations", "caps_release_cache",
-    "caps_leaf_gemm_split_noalloc_dev",
+    "caps_leaf_gemm_split_noalloc_dev", "caps_autotune_entry",
 ]
 
 
@@ -127,6 +127,9 @@ def lib() -> ctypes.CDLL:
         L.caps_release_cache.restype = None
         L.caps_leaf_gemm_split_noalloc_dev.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
         L.caps_leaf_gemm_split_noalloc_dev.restype = ctypes.c_int
+        ip = ctypes.POINTER(ctypes.c_int)
+        L.caps_autotune_entry.argtypes = [ctypes.c_int, ip, ip, ip, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
+        L.caps_autotune_entry.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -236,6 +239,20 @@ def multiply_batched(As, Bs, Cs, ns, form: int | str = CAPS_FORM_PLAIN, slices: 
     _check(lib().caps_multiply_batched_dev(count, ctypes.cast(pa, ctypes.c_void_p), ctypes.cast(pb, ctypes.c_void_p),
                                            ctypes.cast(pc, ctypes.c_void_p), nn, ctypes.byref(opt),
                                            _stream_ptr(stream)))
+
+
+def autotune_table() -> list:
+    """The autotuner's choices so far: dicts of n, form, nrec, pattern, seconds per instance."""
+    out = []
+    i = 0
+    while True:
+        n, f, r, sec = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        pat = ctypes.create_string_buffer(9)
+        if lib().caps_autotune_entry(i, ctypes.byref(n), ctypes.byref(f), ctypes.byref(r), pat, ctypes.byref(sec)):
+            return out
+        out.append({"n": n.value, "form": "split" if f.value == 1 else "plain", "nrec": r.value,
+                    "pattern": pat.value.decode(), "seconds_per_instance": sec.value})
+        i += 1
 
 
 def workspace_size(desc: MatDescriptor, pattern=None, form: int | str = CAPS_FORM_PLAIN,

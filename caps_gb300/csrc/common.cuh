@@ -50,6 +50,16 @@ enum EwOp : int {
     EW_ADD2 = 5,
     // calcCij: C11..C22 from Q1..Q7 (7 inputs, 4 outputs)
     EW_CALC_CIJ = 6,
+    // operand pairs of the memory-lean 'd' step, formed just before their
+    // subproduct; src = A11 A21 A12 A22 B11 B21 B12 B22
+    EW_FORM_T4S4 = 7,  // dst0 = (A21+A22)-A11, dst1 = B22-(B12-B11)
+    EW_FORM_T5S5 = 8,  // dst0 = A11-A21,       dst1 = B22-B12
+    EW_FORM_T3S3 = 9,  // dst0 = A21+A22,       dst1 = B12-B11
+    EW_FORM_S7 = 10,   // dst0 = (B22-(B12-B11))-B21
+    EW_FORM_T6 = 11,   // dst0 = A12-((A21+A22)-A11)
+    // dst0 = src0 ; dst1 = src0 + src2 ; dst2 = src1 + src2
+    // (C21 = U2 ; C22 = U2 + Q3 ; U3 = U1 + Q3)
+    EW_U2_Q3 = 12,
 };
 
 struct EwTask {
@@ -98,6 +108,8 @@ cudaError_t split_needed_slices(void *workspace, int count, int m, int *needed, 
 // f / g exponents, digit count, and the digit planes (finalize + slice).
 cudaError_t launch_split_prep(const LeafTask *tasks_dev, int count, int m, SplitParams p,
                               void *workspace, cudaStream_t stream);
+// Sets the GEMM kernel's attributes (once); call before a stream capture.
+void split_gemm_prepare();
 // The tcgen05 digit-pair GEMM with the exact recombination epilogue.
 cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, SplitParams p,
                               void *workspace, unsigned int *status_dev, cudaStream_t stream);

@@ -110,7 +110,7 @@ static caps_status pinned_reserve(size_t bytes) {
 }
 
 // ------------------------------------------------------------------ plan
-enum OpKind { K_EW = 0, K_LEAF_DMMA, K_LEAF_SPLIT, K_REORDER_LEAF };
+enum OpKind { K_EW = 0, K_LEAF_DMMA, K_LEAF_SPLIT, K_REORDER };
 enum Phase { PH_ADD = 0, PH_MUL = 1, PH_REARRANGE = 2 };
 
 struct Op {
@@ -123,6 +123,7 @@ struct Op {
     size_t toff2;  // second table (reorder dst)
     int m;
     int bs;
+    int nrec;
     bool to_caps;
     size_t split_off;  // workspace offset of the split scratch
     SplitParams sp;
@@ -223,12 +224,14 @@ static void emit_leaf_gemm(Builder &b, const std::vector<Prob> &P, int64_t m) {
 }
 
 static void emit_reorder(Builder &b, const std::vector<const double *> &src,
-                         const std::vector<double *> &dst, int64_t m, int64_t bs, bool to_caps) {
+                         const std::vector<double *> &dst, int64_t m, int64_t bs, bool to_caps,
+                         int nrec = 0) {
     Op o{};
-    o.kind = K_REORDER_LEAF;
+    o.kind = K_REORDER;
     o.count = (int)src.size();
     o.m = (int)m;
     o.bs = (int)bs;
+    o.nrec = nrec;
     o.to_caps = to_caps;
     o.toff = b.table(src);
     o.toff2 = b.table(dst);
@@ -277,18 +280,21 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
     size_t mk = b.mark();
     std::vector<EwTask> st(P.size());
     if (c == 'b' || c == 'B') {
-        // strassenBFS (multiply.cpp:212-310) on one GPU: 7 subproducts as one batch.
+        // strassenBFS (multiply.cpp:212-310) on one GPU: 7 subproducts as one
+        // batch.  Q1..Q4 are written straight into the C quadrants (calcCij
+        // reads all seven products of an element before writing any of its
+        // four results), Q5..Q7 into workspace: 11 quarter buffers per node.
         std::vector<Prob> ch;
         std::vector<EwTask> cij(P.size());
         for (size_t i = 0; i < P.size(); i++) {
             const Prob &p = P[i];
             const double *A11 = p.A, *A21 = p.A + q, *A12 = p.A + 2 * q, *A22 = p.A + 3 * q;
             const double *B11 = p.B, *B21 = p.B + q, *B12 = p.B + 2 * q, *B22 = p.B + 3 * q;
-            double *W = b.alloc(15 * q);
+            double *C11 = p.C, *C21 = p.C + q, *C12 = p.C + 2 * q, *C22 = p.C + 3 * q;
+            double *W = b.alloc(11 * q);
             double *T3 = W, *T4 = W + q, *T5 = W + 2 * q, *T6 = W + 3 * q;
             double *S3 = W + 4 * q, *S4 = W + 5 * q, *S5 = W + 6 * q, *S7 = W + 7 * q;
-            double *Qv[7];
-            for (int k = 0; k < 7; k++) Qv[k] = W + (8 + k) * q;
+            double *Qv[7] = {C11, C12, C21, C22, W + 8 * q, W + 9 * q, W + 10 * q};
             st[i] = EwTask{{A11, A21, A12, A22, B11, B21, B12, B22}, {T3, T4, T5, T6, S3, S4, S5, S7}};
             ch.push_back({A11, B11, Qv[0]});
             ch.push_back({A12, B21, Qv[1]});
@@ -299,24 +305,26 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
             ch.push_back({A22, S7, Qv[6]});
             EwTask t{};
             for (int k = 0; k < 7; k++) t.src[k] = Qv[k];
-            t.dst[0] = p.C;          // C11
-            t.dst[1] = p.C + 2 * q;  // C12
-            t.dst[2] = p.C + q;      // C21
-            t.dst[3] = p.C + 3 * q;  // C22
+            t.dst[0] = C11;
+            t.dst[1] = C12;
+            t.dst[2] = C21;
+            t.dst[3] = C22;
             cij[i] = t;
         }
         emit_ew(b, EW_FORM_ST, st, q);
         build(b, ch, h, nrec - 1, pat + 1);
         emit_ew(b, EW_CALC_CIJ, cij, q);
     } else {
-        // strassenDFS (multiply.cpp:409-454): subproducts in sequence, each
-        // folded into C in the reference's order:
-        //   C11=Q1; U2=U3=C11+Q4; U2+=Q5; C22=U2+Q3, U3+=Q3; C21=U2-Q7;
-        //   C12=U3+Q6; C11+=Q2.
+        // strassenDFS (multiply.cpp:409-454), memory-lean: each operand pair
+        // is formed just before its subproduct into X, Y, the product goes to
+        // Q, and U1 / U2 / U3 live in C quadrants not yet final -- 3 quarter
+        // buffers per node.  Per element the sums, products and their order
+        // are the reference's:
+        //   C11=Q1; C22=C12=U1=C11+Q4; C22=U2=C22+Q5;
+        //   C21=U2, C22=U2+Q3, C12=U3=C12+Q3; C21=U2-Q7; C12=U3+Q6; C11+=Q2.
         struct Nd {
             const double *A11, *A21, *A12, *A22, *B11, *B21, *B12, *B22;
-            double *C11, *C21, *C12, *C22;
-            double *T3, *T4, *T5, *T6, *S3, *S4, *S5, *S7, *Q, *U2, *U3;
+            double *C11, *C21, *C12, *C22, *X, *Y, *Q;
         };
         std::vector<Nd> nd(P.size());
         for (size_t i = 0; i < P.size(); i++) {
@@ -325,25 +333,26 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
             d.A11 = p.A; d.A21 = p.A + q; d.A12 = p.A + 2 * q; d.A22 = p.A + 3 * q;
             d.B11 = p.B; d.B21 = p.B + q; d.B12 = p.B + 2 * q; d.B22 = p.B + 3 * q;
             d.C11 = p.C; d.C21 = p.C + q; d.C12 = p.C + 2 * q; d.C22 = p.C + 3 * q;
-            double *W = b.alloc(11 * q);
-            d.T3 = W; d.T4 = W + q; d.T5 = W + 2 * q; d.T6 = W + 3 * q;
-            d.S3 = W + 4 * q; d.S4 = W + 5 * q; d.S5 = W + 6 * q; d.S7 = W + 7 * q;
-            d.Q = W + 8 * q; d.U2 = W + 9 * q; d.U3 = W + 10 * q;
-            st[i] = EwTask{{d.A11, d.A21, d.A12, d.A22, d.B11, d.B21, d.B12, d.B22},
-                           {d.T3, d.T4, d.T5, d.T6, d.S3, d.S4, d.S5, d.S7}};
+            double *W = b.alloc(3 * q);
+            d.X = W; d.Y = W + q; d.Q = W + 2 * q;
         }
-        emit_ew(b, EW_FORM_ST, st, q);
+        auto form = [&](int op) {
+            std::vector<EwTask> t(nd.size());
+            for (size_t i = 0; i < nd.size(); i++) {
+                const Nd &d = nd[i];
+                t[i] = EwTask{{d.A11, d.A21, d.A12, d.A22, d.B11, d.B21, d.B12, d.B22}, {d.X, d.Y}};
+            }
+            emit_ew(b, op, t, q);
+        };
         auto sub = [&](int which) {
             std::vector<Prob> ch;
             for (const Nd &d : nd) {
                 switch (which) {
                     case 1: ch.push_back({d.A11, d.B11, d.C11}); break;
                     case 2: ch.push_back({d.A12, d.B21, d.Q}); break;
-                    case 3: ch.push_back({d.T3, d.S3, d.Q}); break;
-                    case 4: ch.push_back({d.T4, d.S4, d.Q}); break;
-                    case 5: ch.push_back({d.T5, d.S5, d.Q}); break;
-                    case 6: ch.push_back({d.T6, d.B22, d.Q}); break;
-                    case 7: ch.push_back({d.A22, d.S7, d.Q}); break;
+                    case 3: case 4: case 5: ch.push_back({d.X, d.Y, d.Q}); break;
+                    case 6: ch.push_back({d.X, d.B22, d.Q}); break;
+                    case 7: ch.push_back({d.A22, d.X, d.Q}); break;
                 }
             }
             build(b, ch, h, nrec - 1, pat + 1);
@@ -357,16 +366,21 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
             emit_ew(b, op, t, q);
         };
         sub(1);
+        form(EW_FORM_T4S4);
         sub(4);
-        comb(EW_ADD_DUP, [](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = d.Q; t.dst[0] = d.U2; t.dst[1] = d.U3; });
+        comb(EW_ADD_DUP, [](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = d.Q; t.dst[0] = d.C22; t.dst[1] = d.C12; });
+        form(EW_FORM_T5S5);
         sub(5);
-        comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.U2; t.src[1] = d.Q; t.dst[0] = d.U2; });
+        comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C22; t.src[1] = d.Q; t.dst[0] = d.C22; });
+        form(EW_FORM_T3S3);
         sub(3);
-        comb(EW_ADD2, [](const Nd &d, EwTask &t) { t.src[0] = d.U2; t.src[1] = d.U3; t.src[2] = d.Q; t.dst[0] = d.C22; t.dst[1] = d.U3; });
+        comb(EW_U2_Q3, [](const Nd &d, EwTask &t) { t.src[0] = d.C22; t.src[1] = d.C12; t.src[2] = d.Q; t.dst[0] = d.C21; t.dst[1] = d.C22; t.dst[2] = d.C12; });
+        form(EW_FORM_S7);
         sub(7);
-        comb(EW_SUB, [](const Nd &d, EwTask &t) { t.src[0] = d.U2; t.src[1] = d.Q; t.dst[0] = d.C21; });
+        comb(EW_SUB, [](const Nd &d, EwTask &t) { t.src[0] = d.C21; t.src[1] = d.Q; t.dst[0] = d.C21; });
+        form(EW_FORM_T6);
         sub(6);
-        comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.U3; t.src[1] = d.Q; t.dst[0] = d.C12; });
+        comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C12; t.src[1] = d.Q; t.dst[0] = d.C12; });
         sub(2);
         comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = d.Q; t.dst[0] = d.C11; });
     }
@@ -411,7 +425,7 @@ static caps_status check_opts(const caps_options &o) {
 // Bytes of workspace one level's pattern char costs for a batch of `count`.
 static int64_t level_ws(char c, int64_t n, int64_t count) {
     int64_t q = (n / 2) * (n / 2);
-    return (c == 'b' || c == 'B' ? 15 : 11) * q * 8 * count;
+    return (c == 'b' || c == 'B' ? 11 : 3) * q * 8 * count;
 }
 
 // Chooses a pattern when the caller gives none: 'b' at the deepest levels
@@ -468,15 +482,20 @@ struct KernelTiming {
     double gemm_leaf_m3 = 0;   // sum over launches of count * m^3
 };
 
-static caps_status run_ops(Planned &pl, cudaStream_t s, double *phase_time, KernelTiming *kt) {
-    char *tables = g_arena.ptr + pl.table_off;
-    if (!pl.b.blob.empty()) {
-        CAPS_TRY(pinned_reserve(pl.b.blob.size()));
-        memcpy(g_pinned.ptr, pl.b.blob.data(), pl.b.blob.size());
-        CAPS_CUDA_TRY(cudaMemcpyAsync(tables, g_pinned.ptr, pl.b.blob.size(), cudaMemcpyHostToDevice, s));
-        CAPS_CUDA_TRY(cudaEventRecord(g_pinned.done, s));
-        g_pinned.pending = true;
-    }
+static caps_status upload_tables(const std::vector<uint8_t> &blob, char *dst, cudaStream_t s) {
+    if (blob.empty()) return CAPS_OK;
+    CAPS_TRY(pinned_reserve(blob.size()));
+    memcpy(g_pinned.ptr, blob.data(), blob.size());
+    CAPS_CUDA_TRY(cudaMemcpyAsync(dst, g_pinned.ptr, blob.size(), cudaMemcpyHostToDevice, s));
+    CAPS_CUDA_TRY(cudaEventRecord(g_pinned.done, s));
+    g_pinned.pending = true;
+    return CAPS_OK;
+}
+
+// Launches a plan's ops.  `tables`: the plan's task tables on the device;
+// `ws_base`: the workspace base its offsets refer to.
+static caps_status launch_ops(const std::vector<Op> &ops, char *tables, char *ws_base, cudaStream_t s,
+                              double *phase_time, KernelTiming *kt) {
     struct Rec {
         cudaEvent_t e0, e1;
         int phase;
@@ -488,7 +507,7 @@ static caps_status run_ops(Planned &pl, cudaStream_t s, double *phase_time, Kern
         cudaEventCreate(&e);
         cudaEventRecord(e, s);
     };
-    for (const Op &o : pl.b.ops) {
+    for (const Op &o : ops) {
         const bool timed = phase_time || kt;
         Rec r{nullptr, nullptr, PH_ADD, false, 0.0};
         cudaError_t err = cudaSuccess;
@@ -507,7 +526,7 @@ static caps_status run_ops(Planned &pl, cudaStream_t s, double *phase_time, Kern
                 break;
             case K_LEAF_SPLIT: {
                 const LeafTask *t = reinterpret_cast<const LeafTask *>(tables + o.toff);
-                void *ws = g_arena.ptr + o.split_off;
+                void *ws = ws_base + o.split_off;
                 // scan + prep are timed with the multiply phase but not as GEMM
                 Rec pre{nullptr, nullptr, PH_MUL, false, 0.0};
                 if (timed) ev_begin(pre.e0);
@@ -526,10 +545,10 @@ static caps_status run_ops(Planned &pl, cudaStream_t s, double *phase_time, Kern
                 r.m3 = (double)o.count * o.m * (double)o.m * o.m;
                 break;
             }
-            case K_REORDER_LEAF:
+            case K_REORDER:
                 if (timed) ev_begin(r.e0);
                 err = launch_reorder(reinterpret_cast<const double *const *>(tables + o.toff),
-                                     reinterpret_cast<double *const *>(tables + o.toff2), o.count, o.m, 0,
+                                     reinterpret_cast<double *const *>(tables + o.toff2), o.count, o.m, o.nrec,
                                      o.bs, o.to_caps, s);
                 r.phase = PH_REARRANGE;
                 break;
@@ -560,6 +579,12 @@ static caps_status run_ops(Planned &pl, cudaStream_t s, double *phase_time, Kern
         }
     }
     return CAPS_OK;
+}
+
+static caps_status run_ops(Planned &pl, cudaStream_t s, double *phase_time, KernelTiming *kt) {
+    char *tables = g_arena.ptr + pl.table_off;
+    CAPS_TRY(upload_tables(pl.b.blob, tables, s));
+    return launch_ops(pl.b.ops, tables, g_arena.ptr, s, phase_time, kt);
 }
 
 static caps_status status_buffer() {
@@ -635,6 +660,294 @@ static caps_status multiply_dev_locked(const double *A, const double *B, double 
             if (op.kind == K_LEAF_SPLIT) last = g_arena.ptr + op.split_off;
         CAPS_TRY(check_device_status(s, last));
     }
+    return CAPS_OK;
+}
+
+
+// ------------------------------------------------------------------ batched
+// Independent multiplies of uneven sizes (column-major in and out).  The
+// instances are grouped by size; for each size the autotuner picks the depth
+// and b/d pattern; inputs are reordered to CAPS layout on the device, every
+// instance of a size class runs in one batched recursion (its base case one
+// persistent GEMM launch per launch group), and results are reordered back.
+// The whole sequence is captured once as a CUDA graph and replayed while the
+// same batch (sizes and pointers) comes back.
+
+struct BatchItem {
+    int n;
+    const double *A, *B;
+    double *C;
+};
+
+struct TuneEntry {
+    int n, form, slices;
+    int nrec;
+    char pat[8];
+    double seconds;
+};
+static std::vector<TuneEntry> g_tune;
+
+struct BatchPlan {
+    std::vector<BatchItem> items;
+    int form = 0, slices = 0, diagonals = 0;
+    long long limit = 0;
+    DevBuf buf;
+    std::vector<Op> ops;
+    std::vector<uint8_t> blob;
+    size_t table_off = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long kernels = 0, adds = 0, muls = 0;
+};
+static std::vector<BatchPlan *> g_batch_plans;
+static cudaStream_t g_cap_stream = nullptr;
+
+static void free_plan(BatchPlan *p) {
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->buf.ptr) cudaFree(p->buf.ptr);
+    delete p;
+}
+
+static int max_tune_nrec(int n, int form) {
+    int mmin = form == CAPS_FORM_SPLIT ? 192 : 96;
+    int r = 0;
+    while (r < 3 && (n % (2 << r)) == 0 && (n >> (r + 1)) >= mmin) r++;
+    return r;
+}
+
+static int64_t batch_ws_per_instance(int n, int nrec, const char *pat, int form) {
+    int64_t total = nrec > 0 ? (int64_t)3 * n * n * 8 : 0, count = 1, m = n;
+    for (int k = 0; k < nrec; k++) {
+        total += level_ws(pat[k], m, count);
+        if (pat[k] == 'b' || pat[k] == 'B') count *= 7;
+        m /= 2;
+    }
+    if (form == CAPS_FORM_SPLIT) total += (int64_t)split_workspace_bytes((int)m, (int)count, 8);
+    return total;
+}
+
+struct ClassCfg {
+    int n, nrec;
+    char pat[8];
+};
+
+// Appends the ops of a batch to the builder.
+static void build_batch(Builder &b, const std::vector<BatchItem> &items, const std::vector<ClassCfg> &cfg,
+                        long long budget) {
+    for (const ClassCfg &c : cfg) {
+        std::vector<BatchItem> cls;
+        for (const BatchItem &it : items)
+            if (it.n == c.n) cls.push_back(it);
+        if (cls.empty()) continue;
+        int64_t per = std::max<int64_t>(1, batch_ws_per_instance(c.n, c.nrec, c.pat, b.opt.form));
+        size_t chunk = (size_t)std::max<int64_t>(1, budget / per);
+        for (size_t s0 = 0; s0 < cls.size(); s0 += chunk) {
+            size_t s1 = std::min(cls.size(), s0 + chunk);
+            size_t mk = b.mark();
+            std::vector<Prob> P;
+            std::vector<const double *> ra, rb, rc_src;
+            std::vector<double *> da, db, rc_dst;
+            for (size_t i = s0; i < s1; i++) {
+                const BatchItem &it = cls[i];
+                if (c.nrec == 0) {
+                    P.push_back({it.A, it.B, it.C});
+                    continue;
+                }
+                int64_t nn = (int64_t)it.n * it.n;
+                double *w = b.alloc(3 * nn);
+                P.push_back({w, w + nn, w + 2 * nn});
+                ra.push_back(it.A);
+                da.push_back(w);
+                rb.push_back(it.B);
+                db.push_back(w + nn);
+                rc_src.push_back(w + 2 * nn);
+                rc_dst.push_back(it.C);
+            }
+            if (c.nrec > 0) {
+                emit_reorder(b, ra, da, c.n, 1, true, c.nrec);
+                emit_reorder(b, rb, db, c.n, 1, true, c.nrec);
+            }
+            build(b, P, c.n, c.nrec, c.pat);
+            if (c.nrec > 0) emit_reorder(b, rc_src, rc_dst, c.n, 1, false, c.nrec);
+            b.release(mk);
+        }
+    }
+}
+
+static caps_status plan_batch(BatchPlan &p, const std::vector<ClassCfg> &cfg, const caps_options &o) {
+    long long budget = o.workspace_limit > 0 ? o.workspace_limit : ((long long)48 << 30);
+    Builder dry;
+    dry.opt = o;
+    build_batch(dry, p.items, cfg, budget);
+    size_t ws = (dry.peak + 255) & ~(size_t)255;
+    size_t total = ws + dry.blob.size() + 256;
+    if (!p.buf.ptr || p.buf.size < total) {
+        if (p.buf.ptr) cudaFree(p.buf.ptr);
+        p.buf = DevBuf();
+        CAPS_TRY(ensure(p.buf, total));
+    }
+    Builder real;
+    real.opt = o;
+    real.ws_base = p.buf.ptr;
+    build_batch(real, p.items, cfg, budget);
+    p.ops = real.ops;
+    p.blob = real.blob;
+    p.table_off = ws;
+    p.adds = real.adds;
+    p.muls = real.muls;
+    return CAPS_OK;
+}
+
+__global__ void fill_uniform_kernel(double *p, int64_t n, uint64_t seed) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t z = (uint64_t)i * 0x9E3779B97F4A7C15ull + seed;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        p[i] = (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+    }
+}
+
+static caps_status run_plan_direct(BatchPlan &p, cudaStream_t s) {
+    char *tables = p.buf.ptr + p.table_off;
+    CAPS_TRY(upload_tables(p.blob, tables, s));
+    return launch_ops(p.ops, tables, p.buf.ptr, s, nullptr, nullptr);
+}
+
+// Autotuner: for one size and form, times each candidate depth / pattern on
+// a synthetic batch of that size and keeps the fastest (cached per process).
+static caps_status tune_size(int n, const caps_options &o, ClassCfg &out) {
+    for (const TuneEntry &t : g_tune)
+        if (t.n == n && t.form == o.form && t.slices == o.slices) {
+            out.n = n;
+            out.nrec = t.nrec;
+            memcpy(out.pat, t.pat, sizeof out.pat);
+            return CAPS_OK;
+        }
+    int rmax = max_tune_nrec(n, o.form);
+    int T = (int)std::max<int64_t>(1, std::min<int64_t>(32, ((int64_t)1 << 27) / ((int64_t)n * n)));
+    int64_t nn = (int64_t)n * n;
+    double *data = nullptr;
+    CAPS_TRY(dev_malloc((void **)&data, (size_t)3 * nn * T * sizeof(double)));
+    fill_uniform_kernel<<<1024, 256>>>(data, 3 * nn * T, 12345 + n);
+    std::vector<BatchItem> items;
+    for (int i = 0; i < T; i++) items.push_back({n, data + 3 * nn * i, data + 3 * nn * i + nn, data + 3 * nn * i + 2 * nn});
+    ClassCfg best{n, 0, {0}};
+    double best_t = 1e30;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    caps_status st = CAPS_OK;
+    for (int r = 0; r <= rmax && st == CAPS_OK; r++) {
+        for (int variant = 0; variant < (r >= 2 ? 2 : 1); variant++) {
+            ClassCfg c{n, r, {0}};
+            for (int k = 0; k < r; k++) c.pat[k] = (variant == 1 && k == 0) ? 'd' : 'b';
+            BatchPlan p;
+            p.items = items;
+            st = plan_batch(p, {c}, o);
+            if (st != CAPS_OK) { if (p.buf.ptr) cudaFree(p.buf.ptr); break; }
+            double t = 1e30;
+            for (int rep = 0; rep < 3 && st == CAPS_OK; rep++) {
+                cudaEventRecord(e0, 0);
+                st = run_plan_direct(p, 0);
+                cudaEventRecord(e1, 0);
+                if (cudaEventSynchronize(e1) != cudaSuccess) st = CAPS_ERR_CUDA;
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (rep > 0) t = std::min(t, (double)ms);
+            }
+            if (p.buf.ptr) cudaFree(p.buf.ptr);
+            if (st == CAPS_OK && t < best_t) {
+                best_t = t;
+                best = c;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(data);
+    if (st != CAPS_OK) return st;
+    TuneEntry te{n, o.form, o.slices, best.nrec, {0}, best_t / 1e3 / T};
+    memcpy(te.pat, best.pat, sizeof te.pat);
+    g_tune.push_back(te);
+    out = best;
+    return CAPS_OK;
+}
+
+static bool same_batch(const BatchPlan &p, const std::vector<BatchItem> &items, const caps_options &o) {
+    if (p.form != o.form || p.slices != o.slices || p.diagonals != o.diagonals || p.limit != o.workspace_limit ||
+        p.items.size() != items.size())
+        return false;
+    for (size_t i = 0; i < items.size(); i++)
+        if (p.items[i].n != items[i].n || p.items[i].A != items[i].A || p.items[i].B != items[i].B ||
+            p.items[i].C != items[i].C)
+            return false;
+    return true;
+}
+
+static caps_status multiply_batched_locked(const std::vector<BatchItem> &items, const caps_options &o,
+                                           cudaStream_t stream) {
+    BatchPlan *plan = nullptr;
+    for (BatchPlan *p : g_batch_plans)
+        if (same_batch(*p, items, o)) plan = p;
+    if (!plan) {
+        std::vector<int> sizes;
+        for (const BatchItem &it : items)
+            if (std::find(sizes.begin(), sizes.end(), it.n) == sizes.end()) sizes.push_back(it.n);
+        std::sort(sizes.begin(), sizes.end());
+        std::vector<ClassCfg> cfg;
+        if (o.form == CAPS_FORM_SPLIT) CAPS_TRY(status_buffer());
+        for (int n : sizes) {
+            ClassCfg c;
+            CAPS_TRY(tune_size(n, o, c));
+            cfg.push_back(c);
+        }
+        plan = new BatchPlan();
+        plan->items = items;
+        plan->form = o.form;
+        plan->slices = o.slices;
+        plan->diagonals = o.diagonals;
+        plan->limit = o.workspace_limit;
+        caps_status st = plan_batch(*plan, cfg, o);
+        if (st != CAPS_OK) {
+            free_plan(plan);
+            return st;
+        }
+        // tables go up once, outside the graph
+        char *tables = plan->buf.ptr + plan->table_off;
+        if (!plan->blob.empty())
+            CAPS_CUDA_TRY(cudaMemcpy(tables, plan->blob.data(), plan->blob.size(), cudaMemcpyHostToDevice));
+        if (!g_cap_stream) CAPS_CUDA_TRY(cudaStreamCreateWithFlags(&g_cap_stream, cudaStreamNonBlocking));
+        split_gemm_prepare();
+        long long l0 = g_launches;
+        CAPS_CUDA_TRY(cudaStreamBeginCapture(g_cap_stream, cudaStreamCaptureModeThreadLocal));
+        st = launch_ops(plan->ops, tables, plan->buf.ptr, g_cap_stream, nullptr, nullptr);
+        cudaError_t ce = cudaStreamEndCapture(g_cap_stream, &plan->graph);
+        if (st != CAPS_OK || ce != cudaSuccess) {
+            if (ce != cudaSuccess) note_cuda_error(ce, "cudaStreamEndCapture");
+            free_plan(plan);
+            return st != CAPS_OK ? st : CAPS_ERR_CUDA;
+        }
+        plan->kernels = g_launches - l0;
+        ce = cudaGraphInstantiate(&plan->exec, plan->graph, 0);
+        if (ce != cudaSuccess) {
+            note_cuda_error(ce, "cudaGraphInstantiate");
+            free_plan(plan);
+            return CAPS_ERR_CUDA;
+        }
+        if (g_batch_plans.size() >= 4) {
+            free_plan(g_batch_plans.front());
+            g_batch_plans.erase(g_batch_plans.begin());
+        }
+        g_batch_plans.push_back(plan);
+    }
+    CAPS_CUDA_TRY(cudaGraphLaunch(plan->exec, stream));
+    g_counters.additions = plan->adds;
+    g_counters.multiplications = plan->muls;
+    g_counters.kernel_launches = plan->kernels;
+    if (o.form == CAPS_FORM_SPLIT) CAPS_TRY(check_device_status(stream, nullptr));
+    else CAPS_CUDA_TRY(cudaStreamSynchronize(stream));
     return CAPS_OK;
 }
 
@@ -757,8 +1070,30 @@ const char *caps_last_cuda_error(void) { return g_last_err.c_str(); }
 caps_status caps_multiply_batched_dev(int count, const double *const *A, const double *const *B,
                                       double *const *C, const int *n, const caps_options *opt,
                                       void *stream) {
-    (void)count; (void)A; (void)B; (void)C; (void)n; (void)opt; (void)stream;
-    return CAPS_ERR_UNSUPPORTED;
+    std::lock_guard<std::recursive_mutex> g(g_mu);
+    if (count < 0 || (count > 0 && (!A || !B || !C || !n))) return CAPS_ERR_ARG;
+    caps_options o = opts_or_default(opt);
+    CAPS_TRY(check_opts(o));
+    std::vector<BatchItem> items;
+    for (int i = 0; i < count; i++) {
+        if (n[i] <= 0) return CAPS_ERR_SIZE;
+        if (!A[i] || !B[i] || !C[i]) return CAPS_ERR_ARG;
+        items.push_back({n[i], A[i], B[i], C[i]});
+    }
+    if (items.empty()) return CAPS_OK;
+    return multiply_batched_locked(items, o, (cudaStream_t)stream);
+}
+
+caps_status caps_autotune_entry(int index, int *n, int *form, int *nrec, char *pattern, double *seconds) {
+    std::lock_guard<std::recursive_mutex> g(g_mu);
+    if (index < 0 || index >= (int)g_tune.size()) return CAPS_ERR_ARG;
+    const TuneEntry &t = g_tune[index];
+    if (n) *n = t.n;
+    if (form) *form = t.form;
+    if (nrec) *nrec = t.nrec;
+    if (pattern) memcpy(pattern, t.pat, sizeof t.pat);
+    if (seconds) *seconds = t.seconds;
+    return CAPS_OK;
 }
 
 void caps_debug_fail_allocations(int count) { g_fail_allocs = count > 0 ? count : 0; }
@@ -766,6 +1101,8 @@ void caps_debug_fail_allocations(int count) { g_fail_allocs = count > 0 ? count 
 void caps_release_cache(void) {
     std::lock_guard<std::recursive_mutex> g(g_mu);
     cudaDeviceSynchronize();
+    for (BatchPlan *p : g_batch_plans) free_plan(p);
+    g_batch_plans.clear();
     for (DevBuf *b : {&g_arena, &g_io, &g_status}) {
         if (b->ptr) cudaFree(b->ptr);
         *b = DevBuf();

@@ -47,6 +47,45 @@ __device__ __forceinline__ void calc_cij(const double *q, double *c) {
     c[0] = c11; c[1] = c12; c[2] = c21; c[3] = c22;
 }
 
+// Operand sums of the memory-lean 'd' step: the same formulas, in the same
+// evaluation order, as the reference's (multiply.cpp:421-435).
+template <int OP>
+__device__ __forceinline__ void form_lean(double a11, double a21, double a12, double a22, double b11,
+                                          double b21, double b12, double b22, double &o0, double &o1) {
+    if (OP == EW_FORM_T4S4) {
+        double t3 = a21 + a22;
+        o0 = t3 - a11;
+        double s3 = b12 - b11;
+        o1 = b22 - s3;
+    } else if (OP == EW_FORM_T5S5) {
+        o0 = a11 - a21;
+        o1 = b22 - b12;
+    } else if (OP == EW_FORM_T3S3) {
+        o0 = a21 + a22;
+        o1 = b12 - b11;
+    } else if (OP == EW_FORM_S7) {
+        double s3 = b12 - b11;
+        double s4 = b22 - s3;
+        o0 = s4 - b21;
+        o1 = 0.0;
+    } else {  // EW_FORM_T6
+        double t3 = a21 + a22;
+        double t4 = t3 - a11;
+        o0 = a12 - t4;
+        o1 = 0.0;
+    }
+}
+
+// which of A11 A21 A12 A22 B11 B21 B12 B22 a lean formula reads
+template <int OP>
+__host__ __device__ constexpr bool lean_reads(int k) {
+    return OP == EW_FORM_T4S4   ? (k == 0 || k == 1 || k == 3 || k == 4 || k == 6 || k == 7)
+           : OP == EW_FORM_T5S5 ? (k == 0 || k == 1 || k == 6 || k == 7)
+           : OP == EW_FORM_T3S3 ? (k == 1 || k == 3 || k == 4 || k == 6)
+           : OP == EW_FORM_S7   ? (k == 4 || k == 5 || k == 6 || k == 7)
+                                : (k == 0 || k == 1 || k == 2 || k == 3);
+}
+
 template <int OP>
 __device__ __forceinline__ void ew_scalar(const EwTask &t, int64_t i) {
     if (OP == EW_FORM_ST) {
@@ -78,6 +117,18 @@ __device__ __forceinline__ void ew_scalar(const EwTask &t, int64_t i) {
         calc_cij(q, c);
 #pragma unroll
         for (int k = 0; k < 4; k++) t.dst[k][i] = c[k];
+    } else if (OP >= EW_FORM_T4S4 && OP <= EW_FORM_T6) {
+        double v[8], o0, o1;
+#pragma unroll
+        for (int k = 0; k < 8; k++) v[k] = lean_reads<OP>(k) ? t.src[k][i] : 0.0;
+        form_lean<OP>(v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], o0, o1);
+        t.dst[0][i] = o0;
+        if (OP <= EW_FORM_T3S3) t.dst[1][i] = o1;
+    } else if (OP == EW_U2_Q3) {
+        double u2 = t.src[0][i], u1 = t.src[1][i], q = t.src[2][i];
+        t.dst[0][i] = u2;
+        t.dst[1][i] = u2 + q;
+        t.dst[2][i] = u1 + q;
     }
 }
 
@@ -130,6 +181,22 @@ __device__ __forceinline__ void ew_vec2(const EwTask &t, int64_t i) {
         double2 r1 = make_double2(b.x + q.x, b.y + q.y);
         st2(t.dst[0], i, r0);
         st2(t.dst[1], i, r1);
+    } else if (OP >= EW_FORM_T4S4 && OP <= EW_FORM_T6) {
+        // only the sources the formula reads are loaded
+        double2 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            v[k] = lean_reads<OP>(k) ? ld2(t.src[k], i) : make_double2(0.0, 0.0);
+        double a0, a1, b0, b1;
+        form_lean<OP>(v[0].x, v[1].x, v[2].x, v[3].x, v[4].x, v[5].x, v[6].x, v[7].x, a0, a1);
+        form_lean<OP>(v[0].y, v[1].y, v[2].y, v[3].y, v[4].y, v[5].y, v[6].y, v[7].y, b0, b1);
+        st2(t.dst[0], i, make_double2(a0, b0));
+        if (OP <= EW_FORM_T3S3) st2(t.dst[1], i, make_double2(a1, b1));
+    } else if (OP == EW_U2_Q3) {
+        double2 u2 = ld2(t.src[0], i), u1 = ld2(t.src[1], i), q = ld2(t.src[2], i);
+        st2(t.dst[0], i, u2);
+        st2(t.dst[1], i, make_double2(u2.x + q.x, u2.y + q.y));
+        st2(t.dst[2], i, make_double2(u1.x + q.x, u1.y + q.y));
     }
 }
 
@@ -149,7 +216,9 @@ __global__ void __launch_bounds__(256) ew_kernel(const EwTask *__restrict__ task
 
 static int ew_nsrc(int op) {
     switch (op) {
-        case EW_FORM_ST: return 8;
+        case EW_FORM_ST: case EW_FORM_T4S4: case EW_FORM_T5S5: case EW_FORM_T3S3: case EW_FORM_S7:
+        case EW_FORM_T6: return 8;
+        case EW_U2_Q3: return 3;
         case EW_COPY: return 1;
         case EW_ADD_DUP: case EW_ADD: case EW_SUB: return 2;
         case EW_ADD2: return 3;
@@ -160,7 +229,8 @@ static int ew_nsrc(int op) {
 static int ew_ndst(int op) {
     switch (op) {
         case EW_FORM_ST: return 8;
-        case EW_ADD_DUP: case EW_ADD2: return 2;
+        case EW_ADD_DUP: case EW_ADD2: case EW_FORM_T4S4: case EW_FORM_T5S5: case EW_FORM_T3S3: return 2;
+        case EW_U2_Q3: return 3;
         case EW_CALC_CIJ: return 4;
     }
     return 1;
@@ -199,6 +269,12 @@ cudaError_t launch_elementwise(int op, const EwTask *tasks, int count, int64_t q
             case EW_SUB: launch_op<EW_SUB>(vec, t, c, q, stream); break;
             case EW_ADD2: launch_op<EW_ADD2>(vec, t, c, q, stream); break;
             case EW_CALC_CIJ: launch_op<EW_CALC_CIJ>(vec, t, c, q, stream); break;
+            case EW_FORM_T4S4: launch_op<EW_FORM_T4S4>(vec, t, c, q, stream); break;
+            case EW_FORM_T5S5: launch_op<EW_FORM_T5S5>(vec, t, c, q, stream); break;
+            case EW_FORM_T3S3: launch_op<EW_FORM_T3S3>(vec, t, c, q, stream); break;
+            case EW_FORM_S7: launch_op<EW_FORM_S7>(vec, t, c, q, stream); break;
+            case EW_FORM_T6: launch_op<EW_FORM_T6>(vec, t, c, q, stream); break;
+            case EW_U2_Q3: launch_op<EW_U2_Q3>(vec, t, c, q, stream); break;
             default: return cudaErrorInvalidValue;
         }
         count_launch();

@@ -699,6 +699,21 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 }
 
 static int g_num_sms = 0;
+static cudaError_t g_prepare_error = cudaSuccess;
+static int g_prepared_device = -1;
+
+// Sets the GEMM kernel's shared-memory attribute once per device (also
+// called before a stream capture, where attribute calls are better avoided).
+void split_gemm_prepare() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (g_prepared_device == dev) return;
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_num_sms <= 0) g_num_sms = 152;
+    const size_t smem = (size_t)NSTAGE * STAGE_BYTES + 1024 + 1024;
+    g_prepare_error = cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    g_prepared_device = dev;
+}
 
 cudaError_t launch_split_scan(const LeafTask *tasks_dev, int count, int m, void *workspace,
                               cudaStream_t stream) {
@@ -744,14 +759,9 @@ cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, Split
     Geo g = make_geo(m, count);
     char *ws = (char *)workspace;
     cudaError_t e;
-    if (g_num_sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_num_sms <= 0) g_num_sms = 152;
-    }
-    size_t smem = (size_t)NSTAGE * STAGE_BYTES + 1024 + 1024;
-    e = cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    split_gemm_prepare();
+    const size_t smem = (size_t)NSTAGE * STAGE_BYTES + 1024 + 1024;
+    e = g_prepare_error;
     if (e != cudaSuccess) return e;
     int64_t total = (int64_t)g.mtiles * g.ntiles * count;
     int grid = (int)(total < g_num_sms ? total : g_num_sms);

@@ -140,14 +140,22 @@ void caps_get_counters(caps_counters *out);
 void caps_reset_counters(void);
 void caps_set_phase_timing(int enable);
 
-/* Batched independent multiplies of uneven sizes in one persistent launch
- * per phase (plain or split form), replayed from a CUDA graph when the
- * same batch shape repeats.  Matrices i use A[i], B[i], C[i] (device,
- * column-major n[i] x n[i]).  No reference counterpart (the reference runs
- * one multiply per process). */
+/* Batched independent multiplies of uneven sizes.  Matrices i use A[i],
+ * B[i], C[i] (device, column-major n[i] x n[i]).  Instances are grouped by
+ * size; the autotuner picks recursion depth and b/d pattern per size (timed
+ * on first use, cached per process); each size class runs as one batched
+ * recursion whose base case is a persistent GEMM launch; the whole batch is
+ * captured once as a CUDA graph and replayed while the same sizes and
+ * pointers come back.  Synchronises `stream` before returning.  No
+ * reference counterpart (the reference runs one multiply per process). */
 caps_status caps_multiply_batched_dev(int count, const double *const *A, const double *const *B,
                                       double *const *C, const int *n, const caps_options *opt,
                                       void *stream);
+
+/* Autotuner choices made so far: entry `index` (0, 1, ...) gives the size,
+ * form, recursion depth, pattern (8 bytes) and seconds per instance of the
+ * winning candidate; CAPS_ERR_ARG past the last entry. */
+caps_status caps_autotune_entry(int index, int *n, int *form, int *nrec, char *pattern, double *seconds);
 
 /* Human-readable text of a status. */
 const char *caps_status_string(caps_status s);

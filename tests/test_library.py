@@ -64,8 +64,8 @@ def test_workspace_and_auto_pattern(caps):
     d = caps.MatDescriptor.make(16384, 3)
     q = (8192 ** 2) * 8
     ws_ddd = caps.workspace_size(d, "ddd")
-    # 'd' level keeps 11 quarter buffers: 11 q (n/2) + 11 q/4 + 11 q/16
-    assert ws_ddd >= 11 * q * (1 + 1 / 4 + 1 / 16) * 0.99
+    # a memory-lean 'd' level keeps 3 quarter buffers: 3 q (n/2) + 3 q/4 + 3 q/16
+    assert 3 * q * (1 + 1 / 4 + 1 / 16) * 0.99 <= ws_ddd <= 3 * q * (1 + 1 / 4 + 1 / 16) * 1.01
     ws_bbb = caps.workspace_size(d, "bbb")
     assert ws_bbb > ws_ddd
     # a small budget forces 'd' everywhere, a large one allows 'b' at the bottom
@@ -81,6 +81,10 @@ def test_split_workspace_bounded(caps):
     d = caps.MatDescriptor.make(16384, 3)
     ws = caps.workspace_size(d, "bbb", form="split")
     assert ws < 80 << 30
+    # n = 32768, r = 4, 'bbdd' fits a 120 GB (-m 120000) budget in both forms
+    d5 = caps.MatDescriptor.make(32768, 4)
+    for form in ("split", "plain"):
+        assert caps.workspace_size(d5, "bbdd", form=form) <= 120000 * 2 ** 20
 
 
 @pytest.mark.skipif(not os.path.isfile("/root/reference/randombenchmark.cpp"), reason="reference sources absent")
