@@ -52,6 +52,11 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--samples", type=int, default=256, help="entries checked against binary128")
+    ap.add_argument("--workload", default="split16384",
+                    choices=["split16384", "plain8192", "batched512", "int32768"],
+                    help="split16384: the headline (n=16384, r=3, split vs FP64); plain8192: FP64 Strassen "
+                         "n=8192 r=3 'ddd'; batched512: 512 uneven multiplies; int32768: n=32768 r=4 'bbdd' "
+                         "integers under a 120 GB budget")
     return ap.parse_args()
 
 
@@ -72,14 +77,20 @@ def barrier(world):
         dist.barrier()
 
 
-def max_over_ranks(x: float, world: int) -> float:
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """Slowest rank's time (replicas: every rank runs its own multiplies)."""
     if world <= 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_throughput(units_per_rank: float, world: int, seconds_max: float) -> float:
+    """Whole-job rate: the units all ranks processed over the slowest rank's time."""
+    return world * units_per_rank / seconds_max
 
 
 # ----------------------------------------------------------------- clocks
@@ -239,11 +250,177 @@ def run_reference(args, world, rank):
 
 
 # ----------------------------------------------------------------- GPU legs
+def common_line(metric, value, args, world, ms, config, **extra):
+    d = {"metric": metric, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config}
+    d.update(extra)
+    return d
+
+
+def run_plain8192(args, world, rank, local):
+    """FP64 Strassen n=8192, r=3, 'ddd' on DMMA (uniform[-1,1) inputs)."""
+    import torch
+    import caps_gb300 as cg
+    dev = torch.device("cuda", local)
+    n, r, pat = 8192, 3, "ddd"
+    d = cg.MatDescriptor.make(n, r)
+    g = torch.Generator(device=dev)
+    g.manual_seed(2)
+    A = torch.rand(n * n, dtype=torch.float64, device=dev, generator=g) * 2 - 1
+    B = torch.rand(n * n, dtype=torch.float64, device=dev, generator=g) * 2 - 1
+    C = torch.empty_like(A)
+    for _ in range(args.warmup):
+        cg.multiply(A, B, C, d, pat, form="plain")
+    torch.cuda.synchronize()
+    barrier(world)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            cg.multiply(A, B, C, d, pat, form="plain")
+        e1.record()
+        torch.cuda.synchronize()
+    t = max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps, world)
+    if rank == 0:
+        def cm(x):
+            y = torch.empty_like(x)
+            cg.from_caps_layout(x, y, d)
+            torch.cuda.synchronize()
+            return y.cpu().numpy()
+        err = sampled_error(cm(C), cm(A), cm(B), n, args.samples)
+        print(json.dumps(common_line("effective TFLOP/s (2n³/t), FP64 Strassen n=8192 r=3 'ddd'",
+                                     world * 2.0 * n ** 3 / t / 1e12, args, world, t * 1e3,
+                                     {"workload": "plain FP64 Strassen n=8192 r=3 ddd (DMMA base case)", "n": n,
+                                      "nrec": r, "pattern": pat, "form": "plain",
+                                      "inputs": "uniform[-1,1) seeded"},
+                                     error=err, clocks=clk.summary(),
+                                     gpu_launches=cg.counters()["kernel_launches"] * args.steps)), flush=True)
+
+
+def run_batched512(args, world, rank, local):
+    """512 independent multiplies, n log-uniform over {448, 896, 1792, 3584}."""
+    import numpy as np
+    import torch
+    import caps_gb300 as cg
+    dev = torch.device("cuda", local)
+    rng = np.random.default_rng(5)
+    sizes = [int(x) for x in rng.choice([448, 896, 1792, 3584], 512)]
+    g = torch.Generator(device=dev)
+    g.manual_seed(5 + rank)
+    As = [torch.rand(n * n, dtype=torch.float64, device=dev, generator=g) * 2 - 1 for n in sizes]
+    Bs = [torch.rand(n * n, dtype=torch.float64, device=dev, generator=g) * 2 - 1 for n in sizes]
+    Cs = [torch.empty(n * n, dtype=torch.float64, device=dev) for n in sizes]
+    eff = sum(2.0 * n ** 3 for n in sizes)
+    res = {}
+    for form in ("split", "plain"):
+        steps = args.steps if form == "split" else 1
+        for _ in range(max(1, args.warmup if form == "split" else 1)):  # first call tunes and captures
+            cg.multiply_batched(As, Bs, Cs, sizes, form=form)
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            cg.multiply_batched(As, Bs, Cs, sizes, form=form)  # synchronises
+        t = max_over_ranks((time.perf_counter() - t0) / steps, world)
+        res[form] = {"value": world * eff / t / 1e12, "ms_per_step": t * 1e3, "steps": steps,
+                     "graph_kernels": cg.counters()["kernel_launches"]}
+        if rank == 0:  # error of three instances against binary128
+            res[form]["error"] = {
+                str(sizes[i]): sampled_error(Cs[i].cpu().numpy(), As[i].cpu().numpy(), Bs[i].cpu().numpy(),
+                                             sizes[i], 64) for i in range(3)}
+    if rank == 0:
+        counts = {str(n): sizes.count(n) for n in sorted(set(sizes))}
+        print(json.dumps(common_line("effective TFLOP/s (sum 2n³ / t), 512 uneven multiplies",
+                                     res["split"]["value"], args, world, res["split"]["ms_per_step"],
+                                     {"workload": "512 independent multiplies, n over {448,896,1792,3584}",
+                                      "sizes": counts, "form": "split", "inputs": "uniform[-1,1) seeded",
+                                      "execution": "per-size autotuned depth/pattern, CUDA graph replay"},
+                                     split=res["split"], plain_fp64=res["plain"],
+                                     split_vs_plain=res["split"]["value"] / res["plain"]["value"],
+                                     autotune=cg.autotune_table(),
+                                     gpu_launches=res["split"]["graph_kernels"] * args.steps)), flush=True)
+
+
+def run_int32768(args, world, rank, local):
+    """n=32768, r=4, 'bbdd', integers in [-1024, 1024], 120 GB workspace budget."""
+    import numpy as np
+    import torch
+    import caps_gb300 as cg
+    dev = torch.device("cuda", local)
+    n, r, pat = 32768, 4, "bbdd"
+    budget = 120000 * 2 ** 20
+    d = cg.MatDescriptor.make(n, r)
+    g = torch.Generator(device=dev)
+    g.manual_seed(9)
+    A = torch.randint(-1024, 1025, (n * n,), dtype=torch.int32, device=dev, generator=g).to(torch.float64)
+    B = torch.randint(-1024, 1025, (n * n,), dtype=torch.int32, device=dev, generator=g).to(torch.float64)
+    C = torch.empty_like(A)
+    res = {}
+    for form in ("split", "plain"):
+        steps = args.steps if form == "split" else 1
+        cg.multiply(A, B, C, d, pat, form=form, workspace_limit=budget)
+        torch.cuda.synchronize()
+        cg.set_phase_timing(True)
+        t_tot, add_t, add_b = 0.0, 0.0, 0
+        for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            cg.multiply(A, B, C, d, pat, form=form, workspace_limit=budget)
+            e1.record()
+            torch.cuda.synchronize()
+            c = cg.counters()
+            t_tot += e0.elapsed_time(e1) / 1e3
+            add_t += c["time_add"]
+            add_b += c["add_bytes"]
+        cg.set_phase_timing(False)
+        t = t_tot / steps
+        # bit-exactness on sampled entries: exact int64 dot products
+        y = torch.empty_like(C)
+        cg.from_caps_layout(C, y, d)
+        Ac, Bc = torch.empty_like(A), torch.empty_like(B)
+        cg.from_caps_layout(A, Ac, d)
+        cg.from_caps_layout(B, Bc, d)
+        rng = np.random.default_rng(1)
+        rows, cols = rng.integers(0, n, 64), rng.integers(0, n, 64)
+        Am = Ac.view(n, n)  # [col][row]
+        Bm = Bc.view(n, n)
+        Cm = y.view(n, n)
+        exact = 0
+        for i, j in zip(rows, cols):
+            ref = int((Am[:, i].to(torch.int64) * Bm[j].to(torch.int64)).sum().item())
+            exact += int(float(Cm[j, i].item()) == float(ref))
+        del y, Ac, Bc
+        res[form] = {"value": 2.0 * n ** 3 / t / 1e12, "ms_per_step": t * 1e3, "steps": steps,
+                     "bit_exact_sampled": "%d/64" % exact,
+                     "additions_hbm_gbs": add_b / add_t / 1e9 if add_t > 0 else None,
+                     "workspace_bytes": cg.counters()["workspace_peak_bytes"]}
+    if rank == 0:
+        print(json.dumps(common_line("effective TFLOP/s (2n³/t), n=32768 r=4 'bbdd' integers",
+                                     res["split"]["value"], args, world, res["split"]["ms_per_step"],
+                                     {"workload": "Strassen n=32768 r=4 bbdd, integer inputs [-1024,1024], "
+                                                  "-m 120000 (MB) budget", "n": n, "nrec": r, "pattern": pat,
+                                      "form": "split"},
+                                     split=res["split"], plain_fp64=res["plain"],
+                                     split_vs_plain=res["split"]["value"] / res["plain"]["value"])), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload != "split16384":
+        import torch
+        torch.cuda.set_device(local)
+        from caps_gb300 import build as cbuild
+        if not os.path.exists(cbuild.LIB):
+            cbuild.build()
+        {"plain8192": run_plain8192, "batched512": run_batched512, "int32768": run_int32768}[args.workload](
+            args, world, rank, local)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
         return
     import numpy as np
     import torch
@@ -292,7 +469,7 @@ def main():
     t_split = max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps, world)
     cnt = cg.counters()
     s_used, nd_used = cnt["split_slices"], cnt["split_diagonals"]
-    value = world * 2.0 * n ** 3 / t_split / 1e12
+    value = replica_throughput(2.0 * n ** 3 / 1e12, world, t_split)
 
     # ---- plain FP64 Strassen of the same multiply, and the errors of both
     out = {}

@@ -76,7 +76,8 @@ class Counters(ctypes.Structure):
                 ("time_rearrange", ctypes.c_double), ("workspace_peak_bytes", ctypes.c_longlong),
                 ("split_slices", ctypes.c_int), ("split_diagonals", ctypes.c_int),
                 ("kernel_launches", ctypes.c_longlong), ("time_leaf_gemm", ctypes.c_double),
-                ("leaf_gemm_launches", ctypes.c_longlong), ("leaf_gemm_m3", ctypes.c_double)]
+                ("leaf_gemm_launches", ctypes.c_longlong), ("leaf_gemm_m3", ctypes.c_double),
+                ("add_bytes", ctypes.c_longlong)]
 
 
 _lib = None

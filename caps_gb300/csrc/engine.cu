@@ -142,7 +142,7 @@ struct Builder {
     size_t top = 0, peak = 0;
     int64_t bs = 1;
     caps_options opt;
-    long long adds = 0, muls = 0;
+    long long adds = 0, muls = 0, add_bytes = 0;
     int split_group = 0;
 
     size_t mark() const { return top; }
@@ -176,6 +176,12 @@ static void emit_ew(Builder &b, int op, const std::vector<EwTask> &tasks, int64_
     for (const EwTask &t : tasks) {
         for (int k = 0; k < ns; k++) vec = vec && aligned16(t.src[k]);
         for (int k = 0; k < nd; k++) vec = vec && aligned16(t.dst[k]);
+    }
+    {
+        // algorithmic bytes: the sources each formula reads plus its outputs
+        int reads = ns;
+        if (op >= EW_FORM_T4S4 && op <= EW_FORM_T6) reads = (op == EW_FORM_T4S4) ? 6 : 4;
+        b.add_bytes += (long long)(reads + nd) * q * 8 * (long long)tasks.size();
     }
     Op o{};
     o.kind = K_EW;
@@ -649,6 +655,7 @@ static caps_status multiply_dev_locked(const double *A, const double *B, double 
     g_counters.leaf_gemm_m3 = kt.gemm_leaf_m3;
     g_counters.additions = pl.b.adds;
     g_counters.multiplications = pl.b.muls;
+    g_counters.add_bytes = pl.b.add_bytes;
     g_counters.time_add = pt[PH_ADD];
     g_counters.time_mul = pt[PH_MUL];
     g_counters.time_rearrange = pt[PH_REARRANGE];
@@ -697,7 +704,7 @@ struct BatchPlan {
     size_t table_off = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    long long kernels = 0, adds = 0, muls = 0;
+    long long kernels = 0, adds = 0, muls = 0, add_bytes = 0;
 };
 static std::vector<BatchPlan *> g_batch_plans;
 static cudaStream_t g_cap_stream = nullptr;
@@ -796,6 +803,7 @@ static caps_status plan_batch(BatchPlan &p, const std::vector<ClassCfg> &cfg, co
     p.table_off = ws;
     p.adds = real.adds;
     p.muls = real.muls;
+    p.add_bytes = real.add_bytes;
     return CAPS_OK;
 }
 
@@ -945,6 +953,7 @@ static caps_status multiply_batched_locked(const std::vector<BatchItem> &items, 
     CAPS_CUDA_TRY(cudaGraphLaunch(plan->exec, stream));
     g_counters.additions = plan->adds;
     g_counters.multiplications = plan->muls;
+    g_counters.add_bytes = plan->add_bytes;
     g_counters.kernel_launches = plan->kernels;
     if (o.form == CAPS_FORM_SPLIT) CAPS_TRY(check_device_status(stream, nullptr));
     else CAPS_CUDA_TRY(cudaStreamSynchronize(stream));

@@ -134,6 +134,7 @@ typedef struct caps_counters {
     double time_leaf_gemm;   /* seconds in base-case GEMM kernels alone (phase timing on) */
     long long leaf_gemm_launches;
     double leaf_gemm_m3;     /* sum of leaves * m^3 over those launches */
+    long long add_bytes;     /* algorithmic bytes read + written by the sum / combination kernels */
 } caps_counters;
 
 void caps_get_counters(caps_counters *out);
