@@ -47,12 +47,13 @@ constexpr int TN = 64;          // columns of B per tile (per diagonal region)
 constexpr int TK = 16;          // K per MMA / per pipeline stage
 constexpr int MAXS = 8;         // max digits
 constexpr int CHUNK = 32;       // K16 steps per exact accumulation chunk (K = 512)
-constexpr int NSTAGE = 4;
+constexpr int SUB = 2;           // 16-deep K steps per pipeline stage (K = 32 per stage)
+constexpr int NSTAGE = 2;
 constexpr int A_PLANE_BYTES = TM * TK * 2;  // 4096
 constexpr int B_PLANE_BYTES = TN * TK * 2;  // 2048
-constexpr int STAGE_A = MAXS * A_PLANE_BYTES;
-constexpr int STAGE_B = MAXS * B_PLANE_BYTES;
-constexpr int STAGE_BYTES = STAGE_A + STAGE_B;  // 48 KiB
+constexpr int STAGE_A = SUB * MAXS * A_PLANE_BYTES;
+constexpr int STAGE_B = SUB * MAXS * B_PLANE_BYTES;
+constexpr int STAGE_BYTES = STAGE_A + STAGE_B;  // 96 KiB
 constexpr int GEMM_THREADS = 320;               // producer, MMA, 8 epilogue warps
 constexpr uint32_t WAIT_LIMIT = 1u << 25;
 
@@ -562,7 +563,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             int stage = 0;
             uint32_t phase = 0;
             bool ok = true;
-            uint32_t armed[NSTAGE] = {0, 0, 0, 0};  // 1 + phase of the last arm
+            uint32_t armed[NSTAGE] = {0, 0};  // 1 + phase of the last arm
             for (int64_t tile = blockIdx.x; tile < total && ok; tile += gridDim.x) {
                 int leafi = (int)(tile / tiles_per_leaf);
                 int64_t rem = tile % tiles_per_leaf;
@@ -570,15 +571,20 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                 const char *dg = leaf_digits(ws, g, leafi);
                 const char *srcA = dg + g.off_da + (size_t)mt * g.nks * bytesA;
                 const char *srcB = dg + g.off_db + (size_t)nt * g.nks * bytesB;
-                for (int ks = 0; ks < g.nks; ks++) {
-                    if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, status, 1u)) { ok = false; break; }
-                    mbar_expect_tx(full0 + 8 * stage, bytesA + bytesB);
-                    bulk_g2s(smem_u32(stA + stage * STAGE_A), srcA + (size_t)ks * bytesA, bytesA,
-                             full0 + 8 * stage);
-                    bulk_g2s(smem_u32(stB + stage * STAGE_B), srcB + (size_t)ks * bytesB, bytesB,
-                             full0 + 8 * stage);
-                    armed[stage] = 1 + phase;
-                    if (++stage == NSTAGE) { stage = 0; phase ^= 1; }
+                for (int ch = 0; ch < nchunks && ok; ch++) {
+                    const int ks0 = ch * CHUNK, ks1 = ks0 + CHUNK < g.nks ? ks0 + CHUNK : g.nks;
+                    for (int ks = ks0; ks < ks1; ks += SUB) {
+                        // SUB consecutive 16-deep tiles are adjacent in global memory
+                        const uint32_t nsub = ks + SUB <= ks1 ? SUB : (uint32_t)(ks1 - ks);
+                        if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, status, 1u)) { ok = false; break; }
+                        mbar_expect_tx(full0 + 8 * stage, nsub * (bytesA + bytesB));
+                        bulk_g2s(smem_u32(stA + stage * STAGE_A), srcA + (size_t)ks * bytesA, nsub * bytesA,
+                                 full0 + 8 * stage);
+                        bulk_g2s(smem_u32(stB + stage * STAGE_B), srcB + (size_t)ks * bytesB, nsub * bytesB,
+                                 full0 + 8 * stage);
+                        armed[stage] = 1 + phase;
+                        if (++stage == NSTAGE) { stage = 0; phase ^= 1; }
+                    }
                 }
             }
             // drain: every armed stage's copies must land before exit
@@ -608,16 +614,21 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                     if (!mbar_wait(tempty, (chunk_ctr & 1) ^ 1, status, 4u)) { ok = false; break; }
                     tc_fence_after();
                     int ks0 = ch * CHUNK, ks1 = ks0 + CHUNK < g.nks ? ks0 + CHUNK : g.nks;
-                    for (int ks = ks0; ks < ks1; ks++) {
+                    for (int ks = ks0; ks < ks1; ks += SUB) {
+                        const int nsub = ks + SUB <= ks1 ? SUB : ks1 - ks;
                         if (!mbar_wait(full0 + 8 * stage, phase, status, 8u)) { ok = false; break; }
                         tc_fence_after();
-                        // stage offsets added to the descriptors' address field (>> 4)
-                        const uint64_t soffA = (uint64_t)((uint32_t)(stage * STAGE_A) >> 4);
-                        const uint64_t soffB = (uint64_t)((uint32_t)(stage * STAGE_B) >> 4);
-                        const uint32_t fmask = (ks == ks0) ? tfresh : 0u;
 #pragma unroll
-                        for (int q = 0; q < MAX_MMA; q++)
-                            if (q < nmma) umma(tcol[q], tad[q] + soffA, tbd[q] + soffB, tid[q], ((fmask >> q) & 1u) ^ 1u);
+                        for (int sub = 0; sub < SUB; sub++) {
+                            if (sub >= nsub) break;
+                            // stage and sub-step offsets added to the descriptors' address field (>> 4)
+                            const uint64_t soffA = (uint64_t)((uint32_t)(stage * STAGE_A) + sub * bytesA) >> 4;
+                            const uint64_t soffB = (uint64_t)((uint32_t)(stage * STAGE_B) + sub * bytesB) >> 4;
+                            const uint32_t fmask = (ks == ks0 && sub == 0) ? tfresh : 0u;
+#pragma unroll
+                            for (int q = 0; q < MAX_MMA; q++)
+                                if (q < nmma) umma(tcol[q], tad[q] + soffA, tbd[q] + soffB, tid[q], ((fmask >> q) & 1u) ^ 1u);
+                        }
                         umma_commit(empty0 + 8 * stage);
                         if (++stage == NSTAGE) { stage = 0; phase ^= 1; }
                     }
