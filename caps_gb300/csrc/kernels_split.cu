@@ -162,8 +162,9 @@ __global__ void __launch_bounds__(256) split_scan_kernel(const LeafTask *__restr
         if (i >= M) return;
         int64_t k1 = k0 + KSLAB < M ? k0 + KSLAB : M;
         int emax = -100000, lmin = 100000;
+#pragma unroll 8
         for (int64_t k = k0; k < k1; k++) {
-            double x = t.A[i + k * M];
+            double x = __ldg(t.A + i + k * M);
             if (x != 0.0) {
                 int E, lb;
                 exp_lsb(x, E, lb);
@@ -180,8 +181,9 @@ __global__ void __launch_bounds__(256) split_scan_kernel(const LeafTask *__restr
         int64_t j = (int64_t)blockIdx.x * 8 + w;
         if (j >= M) return;
         int emax = -100000, lmin = 100000;
+#pragma unroll 8
         for (int64_t k = lane; k < M; k += 32) {
-            double x = t.B[k + j * M];
+            double x = __ldg(t.B + k + j * M);
             if (x != 0.0) {
                 int E, lb;
                 exp_lsb(x, E, lb);
@@ -261,17 +263,23 @@ __device__ __forceinline__ long long scaled_round(double x, int f) {
     return (u >> 63) ? -(long long)q : (long long)q;
 }
 
-// balanced base-128 digits of round(x 2^f), most significant first
+// balanced base-128 digits of round(x 2^f), most significant first.
+// X + 64 (1 + 128 + ... + 128^7) has ordinary base-128 digits d_k + 64, so
+// each balanced digit is a 7-bit field minus 64; the top field is not masked
+// (it may reach 128: d_1 = 64 when |X| = 2^55).  Same digits as peeling
+// them off one by one with a carry.
 __device__ __forceinline__ void digits8(double x, int f, int (&d)[8]) {
-    long long R = scaled_round(x, f);
-#pragma unroll
-    for (int k = 7; k >= 0; k--) {
-        long long low = R & 127;
-        if (low >= 64) low -= 128;
-        d[k] = (int)low;
-        R = (R - low) >> 7;
-    }
-    d[0] += (int)(R * 128);
+    const unsigned long long OFF = 0x0081020408102040ull;  // 64 * sum_{k<8} 128^k
+    const unsigned long long U = (unsigned long long)scaled_round(x, f) + OFF;
+    const uint32_t lo = (uint32_t)U, hi = (uint32_t)(U >> 32);
+    d[7] = (int)(lo & 127u) - 64;
+    d[6] = (int)((lo >> 7) & 127u) - 64;
+    d[5] = (int)((lo >> 14) & 127u) - 64;
+    d[4] = (int)((lo >> 21) & 127u) - 64;
+    d[3] = (int)(__funnelshift_r(lo, hi, 28) & 127u) - 64;
+    d[2] = (int)((hi >> 3) & 127u) - 64;
+    d[1] = (int)((hi >> 10) & 127u) - 64;
+    d[0] = (int)(hi >> 17) - 64;
 }
 
 // |d| <= 64 has at most 7 significant bits: 1.5 * 2^23 + d is exact in fp32,
