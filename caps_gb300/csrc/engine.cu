@@ -110,7 +110,13 @@ static caps_status pinned_reserve(size_t bytes) {
 }
 
 // ------------------------------------------------------------------ plan
-enum OpKind { K_EW = 0, K_LEAF_DMMA, K_LEAF_SPLIT, K_REORDER };
+enum OpKind { K_EW = 0, K_LEAF_DMMA, K_LEAF_SPLIT, K_REORDER, K_WAIT, K_RECORD };
+
+// Events the host entry point uses to overlap its copies with a top-level
+// 'd' step: the step waits for A11/B11 (0) before Q1 and for the other input
+// quadrants (1) before forming T4/S4; it records when C22 (2), C21 (3) and
+// C12 (4) are final so their copies back run under the later subproducts.
+constexpr int HOST_EVENTS = 5;
 enum Phase { PH_ADD = 0, PH_MUL = 1, PH_REARRANGE = 2 };
 
 struct Op {
@@ -144,6 +150,7 @@ struct Builder {
     caps_options opt;
     long long adds = 0, muls = 0, add_bytes = 0;
     int split_group = 0;
+    bool host_overlap = false;  // emit K_WAIT / K_RECORD at the top-level 'd' step
 
     size_t mark() const { return top; }
     void release(size_t m) { top = m; }
@@ -190,6 +197,13 @@ static void emit_ew(Builder &b, int op, const std::vector<EwTask> &tasks, int64_
     o.q = q;
     o.count = (int)tasks.size();
     o.toff = b.table(tasks);
+    b.ops.push_back(o);
+}
+
+static void emit_event(Builder &b, int kind, int index) {
+    Op o{};
+    o.kind = kind;
+    o.count = index;
     b.ops.push_back(o);
 }
 
@@ -371,7 +385,10 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
             }
             emit_ew(b, op, t, q);
         };
+        const bool top = b.host_overlap && P.size() == 1 && b.ops.empty();
+        if (top) emit_event(b, K_WAIT, 0);  // A11, B11 on the device
         sub(1);
+        if (top) emit_event(b, K_WAIT, 1);  // the other six input quadrants
         form(EW_FORM_T4S4);
         sub(4);
         comb(EW_ADD_DUP, [](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = d.Q; t.dst[0] = d.C22; t.dst[1] = d.C12; });
@@ -381,12 +398,15 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
         form(EW_FORM_T3S3);
         sub(3);
         comb(EW_U2_Q3, [](const Nd &d, EwTask &t) { t.src[0] = d.C22; t.src[1] = d.C12; t.src[2] = d.Q; t.dst[0] = d.C21; t.dst[1] = d.C22; t.dst[2] = d.C12; });
+        if (top) emit_event(b, K_RECORD, 2);  // C22 final
         form(EW_FORM_S7);
         sub(7);
         comb(EW_SUB, [](const Nd &d, EwTask &t) { t.src[0] = d.C21; t.src[1] = d.Q; t.dst[0] = d.C21; });
+        if (top) emit_event(b, K_RECORD, 3);  // C21 final
         form(EW_FORM_T6);
         sub(6);
         comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C12; t.src[1] = d.Q; t.dst[0] = d.C12; });
+        if (top) emit_event(b, K_RECORD, 4);  // C12 final
         sub(2);
         comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = d.Q; t.dst[0] = d.C11; });
     }
@@ -468,8 +488,10 @@ struct Planned {
 };
 
 static caps_status plan(const double *A, const double *B, double *C, const caps_desc &d,
-                        const char *pat, const caps_options &o, char *ws_base, Planned &pl) {
+                        const char *pat, const caps_options &o, char *ws_base, Planned &pl,
+                        bool host_overlap = false) {
     pl.b = Builder();
+    pl.b.host_overlap = host_overlap;
     pl.b.ws_base = ws_base;
     pl.b.bs = d.bs;
     pl.b.opt = o;
@@ -500,6 +522,8 @@ static caps_status upload_tables(const std::vector<uint8_t> &blob, char *dst, cu
 
 // Launches a plan's ops.  `tables`: the plan's task tables on the device;
 // `ws_base`: the workspace base its offsets refer to.
+static cudaEvent_t g_host_events[HOST_EVENTS];
+
 static caps_status launch_ops(const std::vector<Op> &ops, char *tables, char *ws_base, cudaStream_t s,
                               double *phase_time, KernelTiming *kt) {
     struct Rec {
@@ -551,6 +575,20 @@ static caps_status launch_ops(const std::vector<Op> &ops, char *tables, char *ws
                 r.m3 = (double)o.count * o.m * (double)o.m * o.m;
                 break;
             }
+            case K_WAIT:
+                err = cudaStreamWaitEvent(s, g_host_events[o.count], 0);
+                if (err != cudaSuccess) {
+                    note_cuda_error(err, "cudaStreamWaitEvent");
+                    return CAPS_ERR_CUDA;
+                }
+                continue;
+            case K_RECORD:
+                err = cudaEventRecord(g_host_events[o.count], s);
+                if (err != cudaSuccess) {
+                    note_cuda_error(err, "cudaEventRecord");
+                    return CAPS_ERR_CUDA;
+                }
+                continue;
             case K_REORDER:
                 if (timed) ev_begin(r.e0);
                 err = launch_reorder(reinterpret_cast<const double *const *>(tables + o.toff),
@@ -625,7 +663,7 @@ static caps_status check_device_status(cudaStream_t s, const void *last_split_ws
 
 static caps_status multiply_dev_locked(const double *A, const double *B, double *C, caps_desc d,
                                        const char *pattern, const caps_options &o, cudaStream_t s,
-                                       bool sync_status) {
+                                       bool sync_status, bool host_overlap = false) {
     CAPS_TRY(check_desc(d));
     CAPS_TRY(check_pattern(d, pattern));
     CAPS_TRY(check_opts(o));
@@ -638,14 +676,14 @@ static caps_status multiply_dev_locked(const double *A, const double *B, double 
         auto_pattern(d, o, pat);
     }
     Planned pl;
-    CAPS_TRY(plan(A, B, C, d, pat, o, nullptr, pl));
+    CAPS_TRY(plan(A, B, C, d, pat, o, nullptr, pl, host_overlap));
     if (o.workspace_limit > 0 && (long long)pl.ws_bytes > o.workspace_limit) {
         g_last_err = "workspace of the pattern exceeds the budget";
         return CAPS_ERR_BUDGET;
     }
     if (o.form == CAPS_FORM_SPLIT) CAPS_TRY(status_buffer());
     CAPS_TRY(ensure(g_arena, pl.total));
-    CAPS_TRY(plan(A, B, C, d, pat, o, g_arena.ptr, pl));
+    CAPS_TRY(plan(A, B, C, d, pat, o, g_arena.ptr, pl, host_overlap));
     double pt[3] = {0, 0, 0};
     long long l0 = g_launches;
     KernelTiming kt;
@@ -979,22 +1017,79 @@ caps_status caps_multiply_dev(const double *A, const double *B, double *C, caps_
     return multiply_dev_locked(A, B, C, desc, pattern, opts_or_default(opt), (cudaStream_t)stream, true);
 }
 
+// Host arrays: with a top-level 'd' step (the default when no pattern is
+// given) the copies overlap the computation -- A11, B11 first, the other
+// input quadrants while Q1 runs, and C22 / C21 / C12 back while the later
+// subproducts run (copy stream + events placed in the plan); otherwise all
+// inputs go in before and C comes back after.
 caps_status caps_multiply_host(const double *A, const double *B, double *C, caps_desc desc,
                                const char *pattern, const caps_options *opt) {
     std::lock_guard<std::recursive_mutex> g(g_mu);
     if (!A || !B || !C) return CAPS_ERR_ARG;
     CAPS_TRY(check_desc(desc));
     CAPS_TRY(check_pattern(desc, pattern));
+    caps_options o = opts_or_default(opt);
+    CAPS_TRY(check_opts(o));
+    char pat[32];
+    if (pattern) {
+        for (int l = 0; l < desc.nrec; l++) pat[l] = pattern[l];
+        pat[desc.nrec] = 0;
+    } else {
+        auto_pattern(desc, o, pat);
+        if (desc.nrec > 0) pat[0] = 'd';  // the lean top step lets the copies overlap
+    }
+    const bool overlap = desc.nrec > 0 && (pat[0] == 'd' || pat[0] == 'D' || pat[0] == 'h' || pat[0] == 'H');
     size_t nn = (size_t)desc.lda * desc.lda * sizeof(double);
     size_t slot = (nn + 255) & ~(size_t)255;
     CAPS_TRY(ensure(g_io, 3 * slot));
     double *dA = (double *)g_io.ptr, *dB = (double *)(g_io.ptr + slot), *dC = (double *)(g_io.ptr + 2 * slot);
     cudaStream_t s = 0;
-    CAPS_CUDA_TRY(cudaMemcpyAsync(dA, A, nn, cudaMemcpyHostToDevice, s));
-    CAPS_CUDA_TRY(cudaMemcpyAsync(dB, B, nn, cudaMemcpyHostToDevice, s));
-    CAPS_TRY(multiply_dev_locked(dA, dB, dC, desc, pattern, opts_or_default(opt), s, true));
-    CAPS_CUDA_TRY(cudaMemcpyAsync(C, dC, nn, cudaMemcpyDeviceToHost, s));
+    if (!overlap) {
+        CAPS_CUDA_TRY(cudaMemcpyAsync(dA, A, nn, cudaMemcpyHostToDevice, s));
+        CAPS_CUDA_TRY(cudaMemcpyAsync(dB, B, nn, cudaMemcpyHostToDevice, s));
+        CAPS_TRY(multiply_dev_locked(dA, dB, dC, desc, pat, o, s, true));
+        CAPS_CUDA_TRY(cudaMemcpyAsync(C, dC, nn, cudaMemcpyDeviceToHost, s));
+        CAPS_CUDA_TRY(cudaStreamSynchronize(s));
+        return CAPS_OK;
+    }
+    static cudaStream_t cs = nullptr;
+    static cudaEvent_t start = nullptr;
+    if (!cs) {
+        CAPS_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        CAPS_CUDA_TRY(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+        for (int i = 0; i < HOST_EVENTS; i++)
+            CAPS_CUDA_TRY(cudaEventCreateWithFlags(&g_host_events[i], cudaEventDisableTiming));
+    }
+    const size_t q = nn / 4;  // quadrant bytes: X11, X21, X12, X22 at 0, q, 2q, 3q
+    auto h2d = [&](double *dst, const double *src, int quad) {
+        return cudaMemcpyAsync((char *)dst + quad * q, (const char *)src + quad * q, q, cudaMemcpyHostToDevice, cs);
+    };
+    CAPS_CUDA_TRY(cudaEventRecord(start, s));  // after earlier work on s
+    CAPS_CUDA_TRY(cudaStreamWaitEvent(cs, start, 0));
+    CAPS_CUDA_TRY(h2d(dA, A, 0));
+    CAPS_CUDA_TRY(h2d(dB, B, 0));
+    CAPS_CUDA_TRY(cudaEventRecord(g_host_events[0], cs));
+    for (int quad = 1; quad < 4; quad++) {
+        CAPS_CUDA_TRY(h2d(dA, A, quad));
+        CAPS_CUDA_TRY(h2d(dB, B, quad));
+    }
+    CAPS_CUDA_TRY(cudaEventRecord(g_host_events[1], cs));
+    caps_status st = multiply_dev_locked(dA, dB, dC, desc, pat, o, s, false, true);
+    if (st != CAPS_OK) {
+        cudaStreamSynchronize(cs);
+        return st;
+    }
+    // C22 (quadrant 3), C21 (1), C12 (2) as they become final, C11 (0) at the end
+    const int quad_of_event[5] = {-1, -1, 3, 1, 2};
+    for (int e = 2; e < HOST_EVENTS; e++) {
+        CAPS_CUDA_TRY(cudaStreamWaitEvent(cs, g_host_events[e], 0));
+        int quad = quad_of_event[e];
+        CAPS_CUDA_TRY(cudaMemcpyAsync((char *)C + quad * q, (char *)dC + quad * q, q, cudaMemcpyDeviceToHost, cs));
+    }
+    CAPS_CUDA_TRY(cudaMemcpyAsync(C, dC, q, cudaMemcpyDeviceToHost, s));
+    if (o.form == CAPS_FORM_SPLIT) CAPS_TRY(check_device_status(s, nullptr));
     CAPS_CUDA_TRY(cudaStreamSynchronize(s));
+    CAPS_CUDA_TRY(cudaStreamSynchronize(cs));
     return CAPS_OK;
 }
 

@@ -129,6 +129,22 @@ def test_host_entry_point_matches_device(caps, oracle_mod, cuda):
     assert np.array_equal(mat_of(oracle_mod, c, n, r), (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64))
 
 
+@pytest.mark.parametrize("form", ["plain", "split"])
+def test_host_entry_default_pattern_overlapped_copies(caps, oracle_mod, cuda, form):
+    """No pattern: the library's choice, a top-level 'd' step with the copies
+    overlapping the subproducts.  Integer inputs, exact; and a second call
+    with other inputs (the copy stream and events are reused)."""
+    n, r = 512, 3
+    for seed in (11, 12):
+        rng = np.random.default_rng(seed)
+        A = rng.integers(-100, 101, (n, n)).astype(np.float64)
+        B = rng.integers(-100, 101, (n, n)).astype(np.float64)
+        a, b = caps_of(oracle_mod, A, r), caps_of(oracle_mod, B, r)
+        c = np.full(n * n, np.nan)
+        caps.multiply(a, b, c, caps.MatDescriptor.make(n, r), None, form=form)
+        assert np.array_equal(mat_of(oracle_mod, c, n, r), (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64))
+
+
 def test_counters_after_multiply(caps, oracle_mod, cuda):
     n, r = 256, 2
     A = np.ones((n, n))
