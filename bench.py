@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--slices", type=int, default=0)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-wide", action="store_true", help="skip the wide-range (u*2^k) error check")
     ap.add_argument("--samples", type=int, default=256, help="entries checked against binary128")
     ap.add_argument("--workload", default="split16384",
                     choices=["split16384", "plain8192", "batched512", "int32768"],
@@ -499,6 +500,25 @@ def main():
         out["split_error"] = err_split
         out["plain"] = plain
         del A_cm, B_cm
+        if not args.no_wide:
+            # config 3b: a = u 2^k, u uniform[-1,1), k uniform integer in [-20, 20]
+            gw = torch.Generator(device=dev)
+            gw.manual_seed(4)
+            Aw = (torch.rand(n * n, dtype=torch.float64, device=dev, generator=gw) * 2 - 1) * torch.exp2(
+                torch.randint(-20, 21, (n * n,), device=dev, generator=gw).to(torch.float64))
+            Bw = (torch.rand(n * n, dtype=torch.float64, device=dev, generator=gw) * 2 - 1) * torch.exp2(
+                torch.randint(-20, 21, (n * n,), device=dev, generator=gw).to(torch.float64))
+            Cw = torch.empty_like(Aw)
+            Aw_cm, Bw_cm = colmajor(Aw), colmajor(Bw)
+            wide = {}
+            for form in (("split",) if args.no_plain else ("split", "plain")):
+                cg.multiply(Aw, Bw, Cw, desc, pattern, form=form, slices=args.slices, stream=stream.cuda_stream)
+                torch.cuda.synchronize()
+                wide[form] = sampled_error(colmajor(Cw), Aw_cm, Bw_cm, n, args.samples)
+                if form == "split":
+                    wide["split_slices"] = cg.counters()["split_slices"]
+            out["wide"] = wide
+            del Aw, Bw, Cw, Aw_cm, Bw_cm
 
     # ---- e2e through the host entry point (pinned host buffers)
     hA = torch.empty(n * n, dtype=torch.float64, pin_memory=True)
@@ -549,6 +569,7 @@ def main():
             "split_vs_plain": (value / world) / plain["value"] if plain else None,
             "plain_fp64": plain,
             "error": {"split": out.get("split_error"), "plain": plain["error"] if plain else None,
+                      "wide_range_inputs": out.get("wide"),
                       "definition": "max over sampled (i,j) of |C_ij - C_ref_ij| / (|A||B|)_ij, and "
                                     "||C - C_ref||_2 / ||C_ref||_2 over the same entries; C_ref = binary128 dot"},
             "roofline": {"bound": "tensor", "kernel": "split_gemm_kernel", "achieved": achieved, "peak": peak,

@@ -10,6 +10,36 @@
 #include <cstdlib>
 #include <cstring>
 
+// Whole-file text reading: one read, then strtod over the buffer (the
+// reference reads element by element with fscanf, fromfile1.cpp:45-57, which
+// takes minutes for matrices in the thousands).
+struct TextNumbers {
+    char *buf = nullptr;
+    char *p = nullptr;
+    bool open(const char *path) {
+        FILE *f = fopen(path, "rb");
+        if (!f) return false;
+        fseek(f, 0, SEEK_END);
+        long sz = ftell(f);
+        fseek(f, 0, SEEK_SET);
+        buf = (char *)malloc((size_t)sz + 1);
+        size_t got = fread(buf, 1, (size_t)sz, f);
+        buf[got] = 0;
+        fclose(f);
+        p = buf;
+        return true;
+    }
+    // next number; false at the end of the text or on a token that is not one
+    bool next(double *v) {
+        char *e = nullptr;
+        *v = strtod(p, &e);
+        if (e == p) return false;
+        p = e;
+        return true;
+    }
+    ~TextNumbers() { free(buf); }
+};
+
 static int find_option(int argc, char **argv, const char *option) {
     for (int i = 1; i < argc; i++)
         if (strcmp(argv[i], option) == 0) return i;
@@ -45,26 +75,31 @@ int main(int argc, char **argv) {
         printf("Specify input file\n");
         exit(-1);
     }
-    FILE *f = fopen(inFile, "r");
-    if (!f) {
+    TextNumbers in;
+    if (!in.open(inFile)) {
         printf("Error opening file: %s\n", inFile);
         exit(-1);
     }
-    int reads = 0;
-    reads += fscanf(f, "%d\n", &desc.lda);
+    long long reads = 0;
+    double v;
+    desc.lda = 0;
+    if (in.next(&v)) {
+        desc.lda = (int)v;
+        reads++;
+    }
     long long nn = (long long)desc.lda * desc.lda;
     double *IA = allocate(nn), *IB = allocate(nn);
-    for (int i = 0; i < desc.lda; i++) {
-        for (int j = 0; j < desc.lda; j++) reads += fscanf(f, "%lf ", IA + i + (long long)j * desc.lda);
-        reads += fscanf(f, "\n");
+    for (int M = 0; M < 2; M++) {
+        double *X = M == 0 ? IA : IB;
+        for (int i = 0; i < desc.lda; i++)
+            for (int j = 0; j < desc.lda; j++)
+                if (in.next(&v)) {
+                    X[i + (long long)j * desc.lda] = v;  // row i of the file is row i of the matrix
+                    reads++;
+                }
     }
-    for (int i = 0; i < desc.lda; i++) {
-        for (int j = 0; j < desc.lda; j++) reads += fscanf(f, "%lf ", IB + i + (long long)j * desc.lda);
-        reads += fscanf(f, "\n");
-    }
-    fclose(f);
-    if (reads != desc.lda * desc.lda * 2 + 1) {
-        printf("Error reading file: %s, only read %d entries\n", inFile, reads);
+    if (reads != nn * 2 + 1) {
+        printf("Error reading file: %s, only read %lld entries\n", inFile, reads);
         exit(-1);
     }
     printf("Read complete\n");
@@ -96,15 +131,15 @@ int main(int argc, char **argv) {
     double *OC = allocate(nn);
     collectTo1Proc(desc, OC, C);
     if (checkFile) {
-        FILE *cFile = fopen(checkFile, "r");
-        if (!cFile) {
+        TextNumbers chk;
+        if (!chk.open(checkFile)) {
             printf("Error opening file: %s\n", checkFile);
             exit(-1);
         }
         double CC, error = 0;
         for (int i = 0; i < desc.lda; i++) {
             for (int j = 0; j < desc.lda; j++) {
-                if (fscanf(cFile, "%lf ", &CC) == 1) {
+                if (chk.next(&CC)) {
                     double e = fabs(OC[i + (long long)j * desc.lda] - CC);
                     if (e > error) error = e;
                 } else {
@@ -112,12 +147,7 @@ int main(int argc, char **argv) {
                     exit(-1);
                 }
             }
-            if (fscanf(cFile, "\n")) {
-                printf("Error reading verification file\n");
-                exit(-1);
-            }
         }
-        fclose(cFile);
         printf("Maximum deviation %e\n", error);
     } else {
         FILE *oFile = outFile ? fopen(outFile, "w") : stdout;

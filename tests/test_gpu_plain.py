@@ -218,3 +218,29 @@ def test_randombenchmark_driver(caps, cuda):
     bad = subprocess.run([exe, "-s", "1024", "-r", "2", "-p", "bx"], stdout=subprocess.PIPE,
                          stderr=subprocess.STDOUT, text=True, timeout=300)
     assert bad.returncode != 0 and "Invalid pattern" in bad.stdout
+
+
+def test_fromfile1_on_generated_fixture(caps, cuda, tmp_path):
+    """A 448 fixture from the fixture generator (signed entries, exact product)
+    through bin/fromfile1 at every depth the reference's params would list."""
+    import importlib.util
+    import subprocess
+    spec = importlib.util.spec_from_file_location(
+        "caps_generate_test", os.path.join(ROOT, "caps_gb300", "drivers", "generate_test.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    n = 448
+    base = str(tmp_path / "t448")
+    gen.generate(n, base, lo=-9, hi=9, seed=11)
+    exe = os.path.join(os.path.dirname(caps.LIB_PATH), "..", "bin", "fromfile1")
+    params = gen.valid_params(n)
+    picked = [(bs, r) for bs, r in params if bs in (1, 7, 14, 56) or bs == n >> r]
+    assert any(r == 6 for _, r in picked)
+    for bs, r in picked:
+        for form, pat in (("plain", None), ("split", "bd" * 3)):
+            cmd = [exe, "-i", base + ".in", "-b", str(bs), "-r", str(r), "-c", base + ".correct", "--form", form]
+            if pat and r > 0:
+                cmd += ["-p", pat[:r]]
+            out = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=120)
+            assert out.returncode == 0, out.stdout
+            assert "Maximum deviation 0.000000e+00" in out.stdout, (bs, r, form, out.stdout)
