@@ -173,6 +173,24 @@ def profiled_traffic():
 
 
 # ----------------------------------------------------------------- error
+def pinned_copy_bandwidth(h, d, stream, reps=3):
+    """Plain pinned host<->device copy rates (GB/s) of one input matrix on
+    this box, reported beside the e2e figure, which they bound."""
+    import torch
+    out = {}
+    for name, dst, src in (("h2d", d, h), ("d2h", h, d)):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            dst.copy_(src, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = reps * h.numel() * 8 / (e0.elapsed_time(e1) / 1e3) / 1e9
+    return out
+
+
 def sampled_error(C_cm, A_cm, B_cm, n, samples, seed=7):
     """Max elementwise |C - C_ref| / (|A||B|) and normwise over sampled entries;
     C_ref from binary128 (numpy longdouble) dot products."""
@@ -441,6 +459,12 @@ def main():
     B = torch.rand(n * n, dtype=torch.float64, device=dev, generator=g) * 2 - 1
     C = torch.empty_like(A)
     stream = torch.cuda.current_stream(dev)
+    # host copies of the inputs for the e2e leg, pinned while host memory is fresh
+    hA = torch.empty(n * n, dtype=torch.float64, pin_memory=True)
+    hB = torch.empty(n * n, dtype=torch.float64, pin_memory=True)
+    hC = torch.empty(n * n, dtype=torch.float64, pin_memory=True)
+    hA.copy_(A)
+    hB.copy_(B)
 
     def step(form, c=C):
         cg.multiply(A, B, c, desc, pattern, form=form, slices=args.slices, stream=stream.cuda_stream)
@@ -471,6 +495,23 @@ def main():
     cnt = cg.counters()
     s_used, nd_used = cnt["split_slices"], cnt["split_diagonals"]
     value = replica_throughput(2.0 * n ** 3 / 1e12, world, t_split)
+
+    # ---- e2e through the host entry point (pinned host buffers).  Timed
+    # before the error checks below: their multi-GiB pageable host copies
+    # leave host memory fragmented, and pinned copies made after them ran at
+    # a fraction of the bandwidth measured right after start-up.
+    nA, nB, nC = hA.numpy(), hB.numpy(), hC.numpy()
+    copy_bw = pinned_copy_bandwidth(hA, A, stream)
+    # the call a user makes: no pattern, the library's choice for host arrays
+    # (a top-level 'd' step whose subproducts overlap the copies)
+    e2e_pattern = cg.resolve_pattern(desc, None, form="split", workspace_limit=96 << 30)
+    cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices)
+    t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
+    barrier(world)
 
     # ---- plain FP64 Strassen of the same multiply, and the errors of both
     out = {}
@@ -519,26 +560,7 @@ def main():
                     wide["split_slices"] = cg.counters()["split_slices"]
             out["wide"] = wide
             del Aw, Bw, Cw, Aw_cm, Bw_cm
-
-    # ---- e2e through the host entry point (pinned host buffers)
-    hA = torch.empty(n * n, dtype=torch.float64, pin_memory=True)
-    hB = torch.empty(n * n, dtype=torch.float64, pin_memory=True)
-    hC = torch.empty(n * n, dtype=torch.float64, pin_memory=True)
-    hA.copy_(A)
-    hB.copy_(B)
-    del A, B, C
-    torch.cuda.empty_cache()
-    nA, nB, nC = hA.numpy(), hB.numpy(), hC.numpy()
-    # the call a user makes: no pattern, the library's choice for host arrays
-    # (a top-level 'd' step whose subproducts overlap the copies)
-    e2e_pattern = cg.resolve_pattern(desc, None, form="split", workspace_limit=96 << 30)
-    cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices)
-    barrier(world)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices)
-    t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
-    barrier(world)
+        out["copy_bw_late"] = pinned_copy_bandwidth(hA, A, stream)
 
     if rank == 0:
         peaks, peak_src = measured_peaks()
@@ -581,7 +603,8 @@ def main():
             "cpu_baseline": cpu,
             "e2e": {"value": world * 2.0 * n ** 3 / t_e2e / 1e12, "unit": "TFLOP/s",
                     "h2d_bytes_per_step": 2 * n * n * 8, "d2h_bytes_per_step": n * n * 8,
-                    "ms_per_step": t_e2e * 1e3,
+                    "ms_per_step": t_e2e * 1e3, "pinned_copy_gbs": copy_bw,
+                    "pinned_copy_gbs_after_error_checks": out.get("copy_bw_late"),
                     "api": "caps_multiply_host, pinned host buffers, no pattern given: top level 'd' + %s "
                            "with copies overlapped" % e2e_pattern[1:]},
             "gpu_launches": launches,
