@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Benchmark of the CAPS Strassen multiply on GB300 (one JSON line on rank 0).
 
-Metric: effective TFLOP/s (2 n^3 / t) of the split-digit Strassen multiply at
+Metric: effective TFLOP/s (2 n^3 / t) of the split-form Strassen multiply at
 n = 16384, r = 3 (uniform[-1,1) float64 inputs, seeded), with the plain FP64
 (DMMA) Strassen of the same multiply timed beside it and the error of both
 measured on sampled entries against a binary128 (numpy longdouble on aarch64)
@@ -12,8 +12,10 @@ classical product.
             above the 129 MB L2, so nothing is served from L2 across steps)
   e2e       the same through the host entry point: pinned host A, B copied in,
             C copied out, inside the timed region
-  roofline  the dominant kernel (split_gemm_kernel): digit-pair tensor flops
-            per launch / its average launch time (CUDA events, same stream)
+  roofline  the dominant kernel (the split GEMM of the scheme that ran:
+            crt_gemm_kernel for residues, split_gemm_kernel for digits):
+            its tensor flops per launch / its average launch time (CUDA events,
+            same stream)
   cpu_baseline  the oracle restatement of the reference's CPU path (OpenMP +
             OpenBLAS dgemm) on a bounded sample of the same workload
 
@@ -49,6 +51,8 @@ def parse():
     ap.add_argument("--nrec", type=int, default=3)
     ap.add_argument("--pattern", default=None, help="default: the library's choice")
     ap.add_argument("--slices", type=int, default=0)
+    ap.add_argument("--scheme", default="auto", choices=["auto", "digits", "residues"],
+                    help="split-form operand cut (auto: from the data)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-wide", action="store_true", help="skip the wide-range (u*2^k) error check")
@@ -160,9 +164,9 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def profiled_traffic():
-    """dram bytes per split_gemm launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "split_gemm_kernel_n16384.md")
+def profiled_traffic(kernel="split_gemm_kernel"):
+    """dram bytes per GEMM launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "%s_n16384.md" % kernel)
     try:
         for line in open(p):
             if line.strip().startswith("traffic_bytes_per_launch:"):
@@ -467,7 +471,8 @@ def main():
     hB.copy_(B)
 
     def step(form, c=C):
-        cg.multiply(A, B, c, desc, pattern, form=form, slices=args.slices, stream=stream.cuda_stream)
+        cg.multiply(A, B, c, desc, pattern, form=form, slices=args.slices, stream=stream.cuda_stream,
+                    scheme=args.scheme)
 
     # ---- headline: split form, device resident
     for _ in range(max(args.warmup, 3)):
@@ -493,7 +498,7 @@ def main():
     cg.set_phase_timing(False)
     t_split = max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps, world)
     cnt = cg.counters()
-    s_used, nd_used = cnt["split_slices"], cnt["split_diagonals"]
+    s_used, nd_used, moduli = cnt["split_slices"], cnt["split_diagonals"], cnt["split_moduli"]
     value = replica_throughput(2.0 * n ** 3 / 1e12, world, t_split)
 
     # ---- e2e through the host entry point (pinned host buffers).  Timed
@@ -505,11 +510,11 @@ def main():
     # the call a user makes: no pattern, the library's choice for host arrays
     # (a top-level 'd' step whose subproducts overlap the copies)
     e2e_pattern = cg.resolve_pattern(desc, None, form="split", workspace_limit=96 << 30)
-    cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices)
+    cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices, scheme=args.scheme)
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices)
+        cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices, scheme=args.scheme)
     t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
     barrier(world)
 
@@ -553,23 +558,29 @@ def main():
             Aw_cm, Bw_cm = colmajor(Aw), colmajor(Bw)
             wide = {}
             for form in (("split",) if args.no_plain else ("split", "plain")):
-                cg.multiply(Aw, Bw, Cw, desc, pattern, form=form, slices=args.slices, stream=stream.cuda_stream)
+                cg.multiply(Aw, Bw, Cw, desc, pattern, form=form, slices=args.slices, stream=stream.cuda_stream,
+                            scheme=args.scheme)
                 torch.cuda.synchronize()
                 wide[form] = sampled_error(colmajor(Cw), Aw_cm, Bw_cm, n, args.samples)
                 if form == "split":
-                    wide["split_slices"] = cg.counters()["split_slices"]
+                    wc = cg.counters()
+                    wide["split_slices"], wide["split_moduli"] = wc["split_slices"], wc["split_moduli"]
             out["wide"] = wide
             del Aw, Bw, Cw, Aw_cm, Bw_cm
         out["copy_bw_late"] = pinned_copy_bandwidth(hA, A, stream)
 
     if rank == 0:
         peaks, peak_src = measured_peaks()
-        pairs = cg.digit_pairs(s_used, nd_used)
-        per_launch_flops = 2.0 * pairs * gemm_m3 / max(gemm_launches, 1)
+        pairs = cg.digit_pairs(s_used, nd_used) if not moduli else 0
+        products = moduli if moduli else pairs  # tensor-core products per leaf
+        gemm_kernel = "crt_gemm_kernel" if moduli else "split_gemm_kernel"
+        unit_of_work = ("modular products: %d moduli x 2 m^3 per leaf" % moduli if moduli else
+                        "digit-pair products: %d pairs x 2 m^3 per leaf" % pairs)
+        per_launch_flops = 2.0 * products * gemm_m3 / max(gemm_launches, 1)
         per_launch_s = gemm_t / max(gemm_launches, 1)
         achieved = per_launch_flops / per_launch_s / 1e12 if per_launch_s > 0 else 0.0
         peak = float(peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops", 1700.0)))
-        traffic = profiled_traffic()
+        traffic = profiled_traffic(gemm_kernel)
         cpu = None
         if not args.no_cpu:
             try:
@@ -582,8 +593,10 @@ def main():
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_split * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "CAPS Strassen multiply C=A*B, n=%d, r=%d, split-digit base case" % (n, r),
-                       "n": n, "nrec": r, "pattern": pattern, "form": "split", "slices": s_used,
+            "config": {"workload": "CAPS Strassen multiply C=A*B, n=%d, r=%d, split base case (%s)" % (
+                           n, r, "residues modulo %d moduli" % moduli if moduli else "%d digits" % s_used),
+                       "n": n, "nrec": r, "pattern": pattern, "form": "split",
+                       "scheme": "residues" if moduli else "digits", "moduli": moduli, "slices": s_used,
                        "diagonals": nd_used, "digit_pairs": pairs,
                        "inputs": "float64 uniform[-1,1) seeded (torch.Generator), CAPS layout",
                        "l2": "inputs larger than L2 (each matrix 2 GiB vs 129 MB L2)",
@@ -594,12 +607,12 @@ def main():
                       "wide_range_inputs": out.get("wide"),
                       "definition": "max over sampled (i,j) of |C_ij - C_ref_ij| / (|A||B|)_ij, and "
                                     "||C - C_ref||_2 / ||C_ref||_2 over the same entries; C_ref = binary128 dot"},
-            "roofline": {"bound": "tensor", "kernel": "split_gemm_kernel", "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "tensor", "kernel": gemm_kernel, "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "traffic": traffic,
                          "peak_source": "%s bf16_tflops_sustained (of %s)" % (peak_src, peak_src),
                          "flops_per_launch": per_launch_flops, "launches": gemm_launches,
                          "avg_launch_ms": per_launch_s * 1e3,
-                         "unit_of_work": "digit-pair products: %d pairs x 2 m^3 per leaf" % pairs},
+                         "unit_of_work": unit_of_work},
             "cpu_baseline": cpu,
             "e2e": {"value": world * 2.0 * n ** 3 / t_e2e / 1e12, "unit": "TFLOP/s",
                     "h2d_bytes_per_step": 2 * n * n * 8, "d2h_bytes_per_step": n * n * 8,

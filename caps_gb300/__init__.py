@@ -66,7 +66,7 @@ class MatDescriptor(ctypes.Structure):
 
 class Options(ctypes.Structure):
     _fields_ = [("form", ctypes.c_int), ("slices", ctypes.c_int), ("diagonals", ctypes.c_int),
-                ("reserved0", ctypes.c_int), ("workspace_limit", ctypes.c_longlong),
+                ("split_scheme", ctypes.c_int), ("workspace_limit", ctypes.c_longlong),
                 ("reserved", ctypes.c_longlong * 4)]
 
 
@@ -77,7 +77,7 @@ class Counters(ctypes.Structure):
                 ("split_slices", ctypes.c_int), ("split_diagonals", ctypes.c_int),
                 ("kernel_launches", ctypes.c_longlong), ("time_leaf_gemm", ctypes.c_double),
                 ("leaf_gemm_launches", ctypes.c_longlong), ("leaf_gemm_m3", ctypes.c_double),
-                ("add_bytes", ctypes.c_longlong)]
+                ("add_bytes", ctypes.c_longlong), ("split_moduli", ctypes.c_int), ("split_pad", ctypes.c_int)]
 
 
 _lib = None
@@ -145,13 +145,19 @@ def _check(status: int) -> None:
         raise CapsError(status, msg)
 
 
+SPLIT_SCHEMES = {"auto": 0, "digits": 1, "residues": 2}
+
+
 def options(form: int | str = CAPS_FORM_PLAIN, slices: int = 0, diagonals: int = 0,
-            workspace_limit: int = 0) -> Options:
+            workspace_limit: int = 0, scheme: int | str = 0) -> Options:
     if isinstance(form, str):
         form = {"plain": CAPS_FORM_PLAIN, "split": CAPS_FORM_SPLIT}[form]
+    if isinstance(scheme, str):
+        scheme = SPLIT_SCHEMES[scheme]
     o = Options()
     lib().caps_options_init(ctypes.byref(o))
     o.form, o.slices, o.diagonals, o.workspace_limit = int(form), int(slices), int(diagonals), int(workspace_limit)
+    o.split_scheme = int(scheme)
     return o
 
 
@@ -178,14 +184,16 @@ def _stream_ptr(stream):
 
 
 def multiply(A, B, C, desc: MatDescriptor, pattern=None, form: int | str = CAPS_FORM_PLAIN,
-             slices: int = 0, diagonals: int = 0, workspace_limit: int = 0, stream=None) -> None:
+             slices: int = 0, diagonals: int = 0, workspace_limit: int = 0, stream=None,
+             scheme: int | str = 0) -> None:
     """C = A * B for CAPS-layout matrices (multiply.h:13).
 
     Torch CUDA tensors run asynchronously on `stream` (default: torch's
     current stream); numpy arrays go through the host entry point, which
-    stages the copies and synchronises.
+    stages the copies and synchronises.  scheme: split-form operand cut
+    ("auto", "digits" or "residues").
     """
-    opt = options(form, slices, diagonals, workspace_limit)
+    opt = options(form, slices, diagonals, workspace_limit, scheme)
     if isinstance(A, np.ndarray):
         for x in (A, B, C):
             if x.dtype != np.float64 or not x.flags.c_contiguous:
@@ -199,9 +207,9 @@ def multiply(A, B, C, desc: MatDescriptor, pattern=None, form: int | str = CAPS_
 
 
 def leaf_gemm(A, B, C, m: int, form: int | str = CAPS_FORM_PLAIN, slices: int = 0, diagonals: int = 0,
-              stream=None) -> None:
+              stream=None, scheme: int | str = 0) -> None:
     """Base case alone: column-major m x m C = A * B on the device."""
-    opt = options(form, slices, diagonals)
+    opt = options(form, slices, diagonals, 0, scheme)
     _check(lib().caps_leaf_gemm_dev(_dev_ptr(A, "A"), _dev_ptr(B, "B"), _dev_ptr(C, "C"), int(m),
                                     ctypes.byref(opt), _stream_ptr(stream)))
 
@@ -228,7 +236,8 @@ def from_caps_layout(caps, out, desc: MatDescriptor, stream=None) -> None:
                                            _stream_ptr(stream)))
 
 
-def multiply_batched(As, Bs, Cs, ns, form: int | str = CAPS_FORM_PLAIN, slices: int = 0, stream=None) -> None:
+def multiply_batched(As, Bs, Cs, ns, form: int | str = CAPS_FORM_PLAIN, slices: int = 0, stream=None,
+                     scheme: int | str = 0) -> None:
     """Independent column-major multiplies of uneven sizes (lists of CUDA tensors)."""
     count = len(As)
     arr = ctypes.c_void_p * count
@@ -236,7 +245,7 @@ def multiply_batched(As, Bs, Cs, ns, form: int | str = CAPS_FORM_PLAIN, slices: 
     pb = arr(*[_dev_ptr(b, "B").value for b in Bs])
     pc = arr(*[_dev_ptr(c, "C").value for c in Cs])
     nn = (ctypes.c_int * count)(*[int(n) for n in ns])
-    opt = options(form, slices)
+    opt = options(form, slices, 0, 0, scheme)
     _check(lib().caps_multiply_batched_dev(count, ctypes.cast(pa, ctypes.c_void_p), ctypes.cast(pb, ctypes.c_void_p),
                                            ctypes.cast(pc, ctypes.c_void_p), nn, ctypes.byref(opt),
                                            _stream_ptr(stream)))
@@ -257,17 +266,17 @@ def autotune_table() -> list:
 
 
 def workspace_size(desc: MatDescriptor, pattern=None, form: int | str = CAPS_FORM_PLAIN,
-                   workspace_limit: int = 0) -> int:
+                   workspace_limit: int = 0, scheme: int | str = 0) -> int:
     out = ctypes.c_longlong()
-    opt = options(form, 0, 0, workspace_limit)
+    opt = options(form, 0, 0, workspace_limit, scheme)
     _check(lib().caps_workspace_size(desc, _pat(pattern), ctypes.byref(opt), ctypes.byref(out)))
     return out.value
 
 
 def resolve_pattern(desc: MatDescriptor, pattern=None, form: int | str = CAPS_FORM_PLAIN,
-                    workspace_limit: int = 0) -> str:
+                    workspace_limit: int = 0, scheme: int | str = 0) -> str:
     buf = ctypes.create_string_buffer(desc.nrec + 8)
-    opt = options(form, 0, 0, workspace_limit)
+    opt = options(form, 0, 0, workspace_limit, scheme)
     _check(lib().caps_resolve_pattern(desc, _pat(pattern), ctypes.byref(opt), buf, len(buf)))
     return buf.value.decode()
 

@@ -21,7 +21,8 @@ LIBDIR = os.path.join(PKG, "lib")
 BINDIR = os.path.join(PKG, "bin")
 LIB = os.path.join(LIBDIR, "libcaps_gb300.so")
 
-CU_SOURCES = ["engine.cu", "kernels_elementwise.cu", "kernels_dmma.cu", "kernels_split.cu", "noalloc.cu"]
+CU_SOURCES = ["engine.cu", "kernels_elementwise.cu", "kernels_dmma.cu", "kernels_split.cu", "kernels_crt.cu",
+              "noalloc.cu"]
 CPP_SOURCES = ["compat.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

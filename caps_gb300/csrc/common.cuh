@@ -94,24 +94,46 @@ struct LeafTask {
 // FP64 DMMA GEMM (mma.sync f64): C = A * B for every task.
 cudaError_t launch_dmma_gemm(const LeafTask *tasks_dev, int count, int m, cudaStream_t stream);
 
-// Split form.  Workspace per leaf: see split_workspace_bytes().
+// Split form.  Two schemes share one launch sequence; the kernels agree on
+// the scheme through the launch group's header, written on the device after
+// the exponent scan (no host round trip):
+//   digits   -- balanced base-128 digit slices, digit-pair products
+//               (kernels_split.cu);
+//   residues -- residues modulo up to 17 small coprime moduli, one product per
+//               modulus, exact CRT reconstruction (kernels_crt.cu).
+// Workspace per leaf: see split_workspace_bytes().
 struct SplitParams {
-    int slices;     // digits per operand, 1..8
-    int diagonals;  // digit-pair diagonals kept, <= 8, >= slices
+    int slices;     // digit scheme: digits per operand, 1..8 (0 = from the data)
+    int diagonals;  // digit scheme: digit-pair diagonals kept, <= 8, >= slices
+    int scheme;     // caps_options.split_scheme: 0 automatic, 1 digits, 2 residues
 };
-size_t split_workspace_bytes(int m, int count, int slices);
+size_t split_workspace_bytes(int m, int count, int scheme);
 // Computes per-row / per-column scale exponents and the needed digit count.
-cudaError_t launch_split_scan(const LeafTask *tasks_dev, int count, int m, void *workspace,
+cudaError_t launch_split_scan(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
                              cudaStream_t stream);
 // Reads back the digits needed (max over the batch) from the scan results.
 cudaError_t split_needed_slices(void *workspace, int count, int m, int *needed, cudaStream_t stream);
-// f / g exponents, digit count, and the digit planes (finalize + slice).
+// Exponents, the scheme choice, and the operand slices (digit or residue planes).
 cudaError_t launch_split_prep(const LeafTask *tasks_dev, int count, int m, SplitParams p,
                               void *workspace, cudaStream_t stream);
-// Sets the GEMM kernel's attributes (once); call before a stream capture.
+// Sets the GEMM kernels' attributes and constant tables (once per device);
+// call before a stream capture.
 void split_gemm_prepare();
-// The tcgen05 digit-pair GEMM with the exact recombination epilogue.
+// The tensor-core slice products: the digit-pair GEMM with its exact
+// recombination epilogue, or the per-modulus residue GEMM.
 cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, SplitParams p,
                               void *workspace, unsigned int *status_dev, cudaStream_t stream);
+// Residue scheme only: CRT reconstruction of C from the product residues
+// (returns at once when the digit scheme ran).
+cudaError_t launch_split_combine(const LeafTask *tasks_dev, int count, int m, SplitParams p,
+                                 void *workspace, cudaStream_t stream);
+
+// kernels_crt.cu, called by the launchers above
+cudaError_t crt_prepare();
+cudaError_t launch_crt_resolve(int count, int m, SplitParams p, void *workspace, cudaStream_t stream);
+cudaError_t launch_crt_slice(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
+                             cudaStream_t stream);
+cudaError_t launch_crt_gemm(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
+                            unsigned int *status_dev, int num_sms, cudaStream_t stream);
 
 }  // namespace caps

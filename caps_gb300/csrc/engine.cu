@@ -209,10 +209,13 @@ static void emit_event(Builder &b, int kind, int index) {
 
 static void emit_leaf_gemm(Builder &b, const std::vector<Prob> &P, int64_t m) {
     if (b.opt.form == CAPS_FORM_SPLIT) {
-        // bound split scratch: groups of leaves
-        size_t per = split_workspace_bytes((int)m, 1, 8);
-        size_t cap = (size_t)8 << 30;  // 8 GiB of digit planes per launch group
+        // bound split scratch: groups of leaves (the grid's z extent bounds
+        // the count too)
+        const int scheme = b.opt.split_scheme;
+        size_t per = split_workspace_bytes((int)m, 1, scheme);
+        size_t cap = (size_t)8 << 30;  // 8 GiB of slice planes per launch group
         int g = (int)std::max<size_t>(1, std::min<size_t>(P.size(), cap / std::max<size_t>(per, 1)));
+        g = std::min(g, 65535);
         if (b.split_group > 0) g = std::min(g, b.split_group);
         for (size_t s = 0; s < P.size(); s += g) {
             size_t e = std::min(P.size(), s + g);
@@ -224,11 +227,12 @@ static void emit_leaf_gemm(Builder &b, const std::vector<Prob> &P, int64_t m) {
             o.m = (int)m;
             o.toff = b.table(t);
             size_t mk = b.mark();
-            o.split_off = b.alloc_bytes(split_workspace_bytes((int)m, o.count, 8));
+            o.split_off = b.alloc_bytes(split_workspace_bytes((int)m, o.count, scheme));
             b.release(mk);  // scratch is dead once the launch group has run
             // keep the peak: the alloc above already raised it
             o.sp.slices = b.opt.slices;
             o.sp.diagonals = b.opt.diagonals;
+            o.sp.scheme = scheme;
             b.ops.push_back(o);
         }
     } else {
@@ -445,6 +449,7 @@ static caps_status check_opts(const caps_options &o) {
     if (o.form != CAPS_FORM_PLAIN && o.form != CAPS_FORM_SPLIT) return CAPS_ERR_ARG;
     if (o.slices < 0 || o.slices > 8) return CAPS_ERR_ARG;
     if (o.diagonals < 0 || o.diagonals > 8) return CAPS_ERR_ARG;
+    if (o.split_scheme < CAPS_SPLIT_AUTO || o.split_scheme > CAPS_SPLIT_RESIDUES) return CAPS_ERR_ARG;
     return CAPS_OK;
 }
 
@@ -472,7 +477,8 @@ static void auto_pattern(const caps_desc &d, const caps_options &o, char *out) {
             if (out[k] == 'b' || out[k] == 'B') count *= 7;
             n /= 2;
         }
-        if (o.form == CAPS_FORM_SPLIT) total += (int64_t)std::min<size_t>(split_workspace_bytes((int)n, (int)count, 8), (size_t)8 << 30);
+        if (o.form == CAPS_FORM_SPLIT)
+            total += (int64_t)std::min<size_t>(split_workspace_bytes((int)n, (int)count, o.split_scheme), (size_t)8 << 30);
         if (total > budget) {
             out[l] = 'd';
             break;
@@ -560,7 +566,7 @@ static caps_status launch_ops(const std::vector<Op> &ops, char *tables, char *ws
                 // scan + prep are timed with the multiply phase but not as GEMM
                 Rec pre{nullptr, nullptr, PH_MUL, false, 0.0};
                 if (timed) ev_begin(pre.e0);
-                err = launch_split_scan(t, o.count, o.m, ws, s);
+                err = launch_split_scan(t, o.count, o.m, o.sp, ws, s);
                 if (err == cudaSuccess) err = launch_split_prep(t, o.count, o.m, o.sp, ws, s);
                 if (timed) {
                     cudaEventCreate(&pre.e1);
@@ -573,7 +579,27 @@ static caps_status launch_ops(const std::vector<Op> &ops, char *tables, char *ws
                 r.phase = PH_MUL;
                 r.gemm = true;
                 r.m3 = (double)o.count * o.m * (double)o.m * o.m;
-                break;
+                if (err != cudaSuccess) break;
+                if (timed) {
+                    cudaEventCreate(&r.e1);
+                    cudaEventRecord(r.e1, s);
+                    recs.push_back(r);
+                }
+                // residue scheme: the CRT reconstruction, timed with the
+                // multiply phase but not as GEMM (returns at once for digits)
+                Rec post{nullptr, nullptr, PH_MUL, false, 0.0};
+                if (timed) ev_begin(post.e0);
+                err = launch_split_combine(t, o.count, o.m, o.sp, ws, s);
+                if (err != cudaSuccess) {
+                    note_cuda_error(err, "kernel launch");
+                    return CAPS_ERR_CUDA;
+                }
+                if (timed) {
+                    cudaEventCreate(&post.e1);
+                    cudaEventRecord(post.e1, s);
+                    recs.push_back(post);
+                }
+                continue;
             }
             case K_WAIT:
                 err = cudaStreamWaitEvent(s, g_host_events[o.count], 0);
@@ -640,17 +666,19 @@ static caps_status status_buffer() {
 }
 
 // Reads (and clears) the device status word of the split kernels, and the
-// digit / diagonal counts the last split launch group used.
+// digit / diagonal counts (digit scheme) or the moduli count (residue scheme)
+// the last split launch group used.
 static caps_status check_device_status(cudaStream_t s, const void *last_split_ws) {
     if (!g_status.ptr) return CAPS_OK;
     unsigned h = 0;
-    int sd[3] = {0, 0, 0};
+    int sd[4] = {0, 0, 0, 0};  // needed, digits, diagonals, moduli (split header)
     CAPS_CUDA_TRY(cudaMemcpyAsync(&h, g_status.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     if (last_split_ws)
         CAPS_CUDA_TRY(cudaMemcpyAsync(sd, last_split_ws, sizeof sd, cudaMemcpyDeviceToHost, s));
     CAPS_CUDA_TRY(cudaStreamSynchronize(s));
-    g_counters.split_slices = sd[1];
-    g_counters.split_diagonals = sd[2];
+    g_counters.split_moduli = sd[3];
+    g_counters.split_slices = sd[3] ? 0 : sd[1];
+    g_counters.split_diagonals = sd[3] ? 0 : sd[2];
     if (h != 0) {
         CAPS_CUDA_TRY(cudaMemsetAsync(g_status.ptr, 0, sizeof(unsigned), s));
         char buf[96];
@@ -729,12 +757,13 @@ struct TuneEntry {
     int nrec;
     char pat[8];
     double seconds;
+    int scheme;
 };
 static std::vector<TuneEntry> g_tune;
 
 struct BatchPlan {
     std::vector<BatchItem> items;
-    int form = 0, slices = 0, diagonals = 0;
+    int form = 0, slices = 0, diagonals = 0, scheme = 0;
     long long limit = 0;
     DevBuf buf;
     std::vector<Op> ops;
@@ -761,14 +790,14 @@ static int max_tune_nrec(int n, int form) {
     return r;
 }
 
-static int64_t batch_ws_per_instance(int n, int nrec, const char *pat, int form) {
+static int64_t batch_ws_per_instance(int n, int nrec, const char *pat, int form, int scheme) {
     int64_t total = nrec > 0 ? (int64_t)3 * n * n * 8 : 0, count = 1, m = n;
     for (int k = 0; k < nrec; k++) {
         total += level_ws(pat[k], m, count);
         if (pat[k] == 'b' || pat[k] == 'B') count *= 7;
         m /= 2;
     }
-    if (form == CAPS_FORM_SPLIT) total += (int64_t)split_workspace_bytes((int)m, (int)count, 8);
+    if (form == CAPS_FORM_SPLIT) total += (int64_t)split_workspace_bytes((int)m, (int)count, scheme);
     return total;
 }
 
@@ -785,7 +814,7 @@ static void build_batch(Builder &b, const std::vector<BatchItem> &items, const s
         for (const BatchItem &it : items)
             if (it.n == c.n) cls.push_back(it);
         if (cls.empty()) continue;
-        int64_t per = std::max<int64_t>(1, batch_ws_per_instance(c.n, c.nrec, c.pat, b.opt.form));
+        int64_t per = std::max<int64_t>(1, batch_ws_per_instance(c.n, c.nrec, c.pat, b.opt.form, b.opt.split_scheme));
         size_t chunk = (size_t)std::max<int64_t>(1, budget / per);
         for (size_t s0 = 0; s0 < cls.size(); s0 += chunk) {
             size_t s1 = std::min(cls.size(), s0 + chunk);
@@ -865,7 +894,7 @@ static caps_status run_plan_direct(BatchPlan &p, cudaStream_t s) {
 // a synthetic batch of that size and keeps the fastest (cached per process).
 static caps_status tune_size(int n, const caps_options &o, ClassCfg &out) {
     for (const TuneEntry &t : g_tune)
-        if (t.n == n && t.form == o.form && t.slices == o.slices) {
+        if (t.n == n && t.form == o.form && t.slices == o.slices && t.scheme == o.split_scheme) {
             out.n = n;
             out.nrec = t.nrec;
             memcpy(out.pat, t.pat, sizeof out.pat);
@@ -914,7 +943,7 @@ static caps_status tune_size(int n, const caps_options &o, ClassCfg &out) {
     cudaEventDestroy(e1);
     cudaFree(data);
     if (st != CAPS_OK) return st;
-    TuneEntry te{n, o.form, o.slices, best.nrec, {0}, best_t / 1e3 / T};
+    TuneEntry te{n, o.form, o.slices, best.nrec, {0}, best_t / 1e3 / T, o.split_scheme};
     memcpy(te.pat, best.pat, sizeof te.pat);
     g_tune.push_back(te);
     out = best;
@@ -922,7 +951,8 @@ static caps_status tune_size(int n, const caps_options &o, ClassCfg &out) {
 }
 
 static bool same_batch(const BatchPlan &p, const std::vector<BatchItem> &items, const caps_options &o) {
-    if (p.form != o.form || p.slices != o.slices || p.diagonals != o.diagonals || p.limit != o.workspace_limit ||
+    if (p.form != o.form || p.slices != o.slices || p.diagonals != o.diagonals || p.scheme != o.split_scheme ||
+        p.limit != o.workspace_limit ||
         p.items.size() != items.size())
         return false;
     for (size_t i = 0; i < items.size(); i++)
@@ -953,6 +983,7 @@ static caps_status multiply_batched_locked(const std::vector<BatchItem> &items, 
         plan->items = items;
         plan->form = o.form;
         plan->slices = o.slices;
+        plan->scheme = o.split_scheme;
         plan->diagonals = o.diagonals;
         plan->limit = o.workspace_limit;
         caps_status st = plan_batch(*plan, cfg, o);

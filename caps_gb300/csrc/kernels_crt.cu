@@ -1,0 +1,647 @@
+// Residue scheme of the split base case (Ozaki scheme II: an integer modular
+// technique), on tcgen05 tensor cores.
+//
+// The reference multiplies leaves with FP64 dgemm (multiply.cpp:1124,
+// dgemm-blas.cpp:4-13).  This scheme computes the same leaf product
+// C = A * B (column-major m x m, m <= 2048) as follows:
+//
+//  1. scale (shared with the digit scheme): per row i of A the exponent
+//     bound E_i and lowest set bit, per column j of B the same; t_a, t_b =
+//     min(bits needed over the launch group, 55);
+//     A'_ik = round(a_ik 2^(t_a - E_i)), B'_kj = round(b_kj 2^(t_b - E_j)),
+//     |A'| <= 2^t_a, |B'| <= 2^t_b, exact when the data needs <= t bits.
+//  2. resolve: the fewest moduli L whose product M_L exceeds
+//     2 * K * 2^(t_a + t_b) (so C' = A'B' is fixed by its residues), and the
+//     scheme: residues when L + 3 < the digit scheme's digit-pair count.
+//  3. slice:   residues of A', B' modulo the pairwise coprime moduli
+//     p_l in {181, 180, 179, 173, ...} (balanced, |r| <= 90, exact in bf16),
+//     written as pre-tiled UMMA canonical K-major planes like the digits.
+//  4. gemm:    per modulus, sum_k rA rB on tcgen05.mma kind::f16
+//     (bf16 x bf16 -> f32): |sum| <= K 90^2 < 2^24 for K <= 2048, so the
+//     fp32 accumulator is exact.  The epilogue reduces it modulo p_l and
+//     stores z_l = (c mod p_l) y_l mod p_l, y_l = (M_L / p_l)^-1 mod p_l,
+//     one byte per element.
+//  5. combine: S = sum_l z_l (M_L / p_l) < L M_L is reduced modulo M_L and
+//     centred into (-M_L/2, M_L/2): that is C' exactly; then
+//     C = C' 2^(E_i + E_j - t_a - t_b) with one rounding to FP64.
+//
+// Against the digit scheme's 36 digit-pair products for float data, this
+// takes 17 modular products for the same 55-bit operand truncation, and its
+// product of the truncated operands is exact (no dropped digit pairs).
+#include "split_common.cuh"
+
+namespace caps {
+
+using namespace split;
+
+namespace {
+
+// moduli, largest first; any prefix is pairwise coprime
+constexpr int MODULI[LMAX] = {181, 180, 179, 173, 169, 167, 163, 161, 157,
+                              151, 149, 139, 137, 131, 127, 121, 113};
+
+constexpr int RSTAGE_K = 4;                       // 16-deep K steps per stage (K = 64)
+constexpr int RNSTAGE = 4;
+constexpr int RA_TILE = TM * TK * 2;              // 4 KiB: 128 x 16 bf16
+constexpr int RB_TILE = RTN * TK * 2;             // 8 KiB: 256 x 16 bf16
+constexpr int RSTAGE_A = RSTAGE_K * RA_TILE;      // 16 KiB
+constexpr int RSTAGE_B = RSTAGE_K * RB_TILE;      // 32 KiB
+constexpr int RSTAGE_BYTES = RSTAGE_A + RSTAGE_B; // 48 KiB
+constexpr int RGEMM_THREADS = 320;                // producer, MMA, 8 epilogue warps
+constexpr unsigned RSTATUS = 0x100;               // status bits of this kernel: RSTATUS << code
+
+struct CrtTables {
+    float p[LMAX], invp[LMAX];
+    float c[LMAX][3];              // balanced 2^(14k) mod p_l, k = 1..3
+    int lg[LMAX + 1];              // lg[L] = floor(log2 M_L)
+    float y[LMAX][LMAX];           // [L-1][l]: (M_L / p_l)^-1 mod p_l
+    uint32_t Ml[LMAX][LMAX][4];    // [L-1][l]: limbs of M_L / p_l, least significant first
+    uint32_t M[LMAX][4];           // [L-1]: limbs of M_L
+    float m_inv[LMAX];             // [L-1]: 1 / M_L
+};
+
+__constant__ CrtTables c_crt;
+
+typedef unsigned __int128 u128;
+
+int mod_inverse(int a, int p) {
+    a %= p;
+    for (int x = 1; x < p; x++)
+        if ((a * x) % p == 1) return x;
+    return 0;
+}
+
+void build_tables(CrtTables &t) {
+    for (int l = 0; l < LMAX; l++) {
+        const int p = MODULI[l];
+        t.p[l] = (float)p;
+        t.invp[l] = 1.0f / (float)p;
+        long long v = 1;
+        for (int k = 1; k <= 3; k++) {
+            v = (v * 16384) % p;
+            long long b = v > p / 2 ? v - p : v;
+            t.c[l][k - 1] = (float)b;
+        }
+    }
+    t.lg[0] = 0;
+    for (int L = 1; L <= LMAX; L++) {
+        u128 M = 1;
+        for (int l = 0; l < L; l++) M *= (u128)MODULI[l];
+        int lg = 0;
+        while ((M >> (lg + 1)) != 0) lg++;
+        t.lg[L] = lg;
+        for (int k = 0; k < 4; k++) t.M[L - 1][k] = (uint32_t)(M >> (32 * k));
+        t.m_inv[L - 1] = (float)(1.0 / (double)M);
+        for (int l = 0; l < LMAX; l++) {
+            if (l >= L) {
+                t.y[L - 1][l] = 0.0f;
+                for (int k = 0; k < 4; k++) t.Ml[L - 1][l][k] = 0;
+                continue;
+            }
+            const u128 Ml = M / (u128)MODULI[l];
+            t.y[L - 1][l] = (float)mod_inverse((int)(Ml % (u128)MODULI[l]), MODULI[l]);
+            for (int k = 0; k < 4; k++) t.Ml[L - 1][l][k] = (uint32_t)(Ml >> (32 * k));
+        }
+    }
+}
+
+__device__ __forceinline__ int digit_pairs(int s, int nd) {
+    int n = 0;
+    for (int a = 1; a <= s; a++) {
+        int j = s < nd + 1 - a ? s : nd + 1 - a;
+        n += j > 0 ? j : 0;
+    }
+    return n;
+}
+
+// 1.5 * 2^23: adding it to a float of magnitude below 2^22 rounds that float
+// to an integer (one rounding of the exact sum), and the low bits of the
+// sum's encoding then hold the integer.  Keeps rounding and int <-> float
+// conversion on the FMA pipe instead of the conversion unit.
+constexpr float MAGIC = 12582912.0f;
+
+__device__ __forceinline__ float small_int_to_float(int a) {  // |a| < 2^22
+    return __int_as_float(0x4B400000 + a) - MAGIC;
+}
+
+// Residues of X = round(x 2^f) modulo the first L moduli, balanced
+// (|r| <= 90).  X (|X| <= 2^55) is cut into four balanced 14-bit limbs a_k
+// (X + 8192 (1 + 2^14 + 2^28 + 2^42) has ordinary base-16384 digits
+// a_k + 8192; |a_k| <= 8192); then y = sum_k a_k (2^(14k) mod p), balanced,
+// has |y| < 2^21.1 and is exact in fp32, and r = y - p q with q = y * fl(1/p)
+// rounded to an integer by one fused multiply-add with MAGIC.  That product
+// is within |y / p| 2^-24 <= 2^-9.7 of y / p, while y / p lies at least
+// 1/(2p) >= 2^-8.5 from a half-integer (or exactly on one for p = 180, where
+// either neighbour gives |r| = 90), so q is a nearest integer and |r| <= p/2.
+struct Limbs {
+    float a[4];
+};
+
+__device__ __forceinline__ Limbs limbs14(long long X) {
+    const unsigned long long OFF = 0x0080020008002000ull;  // 8192 * sum_{k<4} 16384^k
+    const unsigned long long U = (unsigned long long)X + OFF;
+    Limbs l;
+    l.a[0] = small_int_to_float((int)(U & 16383u) - 8192);
+    l.a[1] = small_int_to_float((int)((U >> 14) & 16383u) - 8192);
+    l.a[2] = small_int_to_float((int)((U >> 28) & 16383u) - 8192);
+    l.a[3] = small_int_to_float((int)(U >> 42) - 8192);
+    return l;
+}
+
+// the balanced residue of x's integer modulo p_l, as an fp32 value (|r| <= 90)
+__device__ __forceinline__ float residue_f32(const Limbs &x, int l) {
+    const float y = fmaf(x.a[3], c_crt.c[l][2], fmaf(x.a[2], c_crt.c[l][1], fmaf(x.a[1], c_crt.c[l][0], x.a[0])));
+    const float q = fmaf(y, c_crt.invp[l], MAGIC) - MAGIC;
+    return fmaf(-q, c_crt.p[l], y);
+}
+
+// two residues as packed bf16: |r| <= 90 has at most 7 significant bits, so
+// the top half of its fp32 encoding is its exact bf16 encoding
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- resolve
+// One thread: picks the scheme for the launch group from the scan's results
+// and writes it into the header, where every later kernel of the group reads it.
+__global__ void crt_resolve_kernel(char *__restrict__ ws, Geo g, SplitParams p) {
+    if (threadIdx.x != 0) return;
+    SplitHdr *h = reinterpret_cast<SplitHdr *>(ws);
+    int s, nd;
+    resolve_sd(h, p, s, nd);
+    h->s_used = s;
+    h->nd_used = nd;
+    const int ta = h->bitsA < 55 ? h->bitsA : 55, tb = h->bitsB < 55 ? h->bitsB : 55;
+    int residues = 0, L = 0;
+    const bool forced_digits = p.scheme == SCHEME_DIGITS || (p.scheme == SCHEME_AUTO && p.slices > 0);
+    if (g.residues_ok && !forced_digits) {
+        int kb = 0;
+        while ((1 << kb) < g.Kp) kb++;
+        const int need = ta + tb + kb + 1;  // K 2^(ta+tb) < M_L / 2
+        L = 1;
+        while (L <= LMAX && c_crt.lg[L] < need) L++;
+        if (L <= LMAX && (p.scheme == SCHEME_RESIDUES || L + 3 < digit_pairs(s, nd))) residues = 1;
+    }
+    h->ta = ta;
+    h->tb = tb;
+    h->moduli = residues ? L : 0;
+    h->residues = residues;
+}
+
+// ---------------------------------------------------------------- slice
+// Residue planes, per modulus l:
+//   A: [l][mt][ks] tiles of 128 x 16 (4 KiB), B: [l][rt][ks] tiles of 256 x 16
+//   (8 KiB), each the UMMA canonical K-major image (8-row x 16-byte core
+//   matrices, K halves side by side: K stride 128 B, row-group stride 256 B).
+// A side: one thread = one row x 8 k, a block = one 128 x 16 tile.  B side:
+// one thread = one column x 8 k, a block = half of a 256 x 16 tile.
+__global__ void __launch_bounds__(256) crt_slice_kernel(const LeafTask *__restrict__ tasks,
+                                                        char *__restrict__ ws, Geo g) {
+    const SplitHdr *h = reinterpret_cast<const SplitHdr *>(ws);
+    if (!h->residues) return;  // the digit scheme runs
+    const int L = h->moduli;
+    const LeafTask t = tasks[blockIdx.z];
+    const char *sc = leaf_scalars(ws, g, blockIdx.z);
+    char *pl = leaf_digits(ws, g, blockIdx.z);
+    const int64_t M = g.m;
+    const int tid = threadIdx.x;
+    const int64_t tile = blockIdx.x;
+    const int kg = tid >> 7;  // which 8 of the tile's 16 k
+    int64_t idx, k0, sk;      // row of A / column of B, first k, stride between k
+    const double *src;
+    int ee, tt;
+    char *dst;
+    size_t plane_stride;
+    if (blockIdx.y == 0) {
+        if (tile >= (int64_t)g.mtiles * g.nks) return;
+        const int mt = (int)(tile / g.nks), ks = (int)(tile % g.nks);
+        const int r = tid & 127;
+        idx = (int64_t)mt * TM + r;
+        k0 = (int64_t)ks * TK + kg * 8;
+        src = t.A + idx + k0 * M;
+        sk = M;
+        ee = idx < M ? reinterpret_cast<const int *>(sc + g.off_ea)[idx] : 0;
+        tt = h->ta;
+        dst = pl + g.off_ra + ((size_t)mt * g.nks + ks) * RA_TILE + (size_t)(r >> 3) * 256 + (size_t)kg * 128 +
+              (size_t)(r & 7) * 16;
+        plane_stride = (size_t)g.mtiles * g.nks * RA_TILE;
+    } else {
+        if (tile >= (int64_t)g.rtiles * g.nks * 2) return;
+        const int64_t bt = tile >> 1;
+        const int rt = (int)(bt / g.nks), ks = (int)(bt % g.nks);
+        const int c = (int)(tile & 1) * 128 + (tid & 127);
+        idx = (int64_t)rt * RTN + c;
+        k0 = (int64_t)ks * TK + kg * 8;
+        src = t.B + k0 + idx * M;
+        sk = 1;
+        ee = idx < M ? reinterpret_cast<const int *>(sc + g.off_eb)[idx] : 0;
+        tt = h->tb;
+        dst = pl + g.off_rb + ((size_t)rt * g.nks + ks) * RB_TILE + (size_t)(c >> 3) * 256 + (size_t)kg * 128 +
+              (size_t)(c & 7) * 16;
+        plane_stride = (size_t)g.rtiles * g.nks * RB_TILE;
+    }
+    // f = t - E (ee = E + 4096; 0 for a zero row / column); padding rows,
+    // columns and k give zero residues
+    const bool live = idx < M && ee != 0;
+    const int f = tt - (ee - 4096);
+    double v[8];
+#pragma unroll
+    for (int e = 0; e < 8; e++) v[e] = (live && k0 + e < M) ? __ldg(src + e * sk) : 0.0;
+    Limbs x[8];
+#pragma unroll
+    for (int e = 0; e < 8; e++) x[e] = limbs14(scaled_round(v[e], f));
+#pragma unroll 1
+    for (int l = 0; l < L; l++) {
+        uint32_t w[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) w[q] = pack_bf16x2(residue_f32(x[2 * q], l), residue_f32(x[2 * q + 1], l));
+        *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+}
+
+// ---------------------------------------------------------------- gemm
+// Persistent, one CTA per SM, 320 threads: warp 0 loads (one lane, bulk
+// copies of pre-tiled planes), warp 1 issues the MMAs (one lane), warps 2..9
+// drain the accumulators.  A work unit is (leaf, modulus, 128-row tile,
+// 256-column tile): Kp / 16 MMAs of 128 x 256 x 16 into one of two TMEM
+// accumulators of 256 columns, so the epilogue drains one unit while the
+// next accumulates.  Units are ordered leaf, modulus, row tile, column tile:
+// the CTAs running at one time share the A and B planes of one modulus of
+// one leaf (16 MB at m = 2048) through L2.
+__global__ void __launch_bounds__(RGEMM_THREADS, 1)
+    crt_gemm_kernel(char *__restrict__ ws, Geo g, unsigned *__restrict__ status) {
+    const SplitHdr *h = reinterpret_cast<const SplitHdr *>(ws);
+    if (!h->residues) return;  // the digit scheme runs
+    const int L = h->moduli;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char *stA = smem;                        // RNSTAGE x RSTAGE_A
+    unsigned char *stB = smem + RNSTAGE * RSTAGE_A;   // RNSTAGE x RSTAGE_B
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + RNSTAGE * RSTAGE_BYTES);
+    // bars: full[RNSTAGE], empty[RNSTAGE], tfull[2], tempty[2], final
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * RNSTAGE + 5);
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + RNSTAGE);
+    const uint32_t tfull0 = smem_u32(bars + 2 * RNSTAGE), tempty0 = smem_u32(bars + 2 * RNSTAGE + 2);
+    const uint32_t finalb = smem_u32(bars + 2 * RNSTAGE + 4);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < RNSTAGE; i++) {
+            mbar_init(full0 + 8 * i, 1);
+            mbar_init(empty0 + 8 * i, 1);
+        }
+        for (int i = 0; i < 2; i++) {
+            mbar_init(tfull0 + 8 * i, 1);
+            mbar_init(tempty0 + 8 * i, 8);
+        }
+        mbar_init(finalb, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
+                         smem_u32(tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    const int64_t tiles = (int64_t)g.mtiles * g.rtiles;
+    const int64_t per_leaf = tiles * L;
+    const int64_t total = per_leaf * g.count;
+    const int nks = g.nks;
+
+    if (warp == 0) {
+        // ------------------------------------------------ producer
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            bool ok = true;
+            uint32_t armed[RNSTAGE] = {0, 0, 0, 0};  // 1 + phase of the last arm
+            for (int64_t u = blockIdx.x; u < total && ok; u += gridDim.x) {
+                const int leafi = (int)(u / per_leaf);
+                const int64_t rem = u % per_leaf;
+                const int l = (int)(rem / tiles);
+                const int64_t tile = rem % tiles;
+                const int mt = (int)(tile / g.rtiles), rt = (int)(tile % g.rtiles);
+                const char *pl = leaf_digits(ws, g, leafi);
+                const char *srcA = pl + g.off_ra + (((size_t)l * g.mtiles + mt) * nks) * RA_TILE;
+                const char *srcB = pl + g.off_rb + (((size_t)l * g.rtiles + rt) * nks) * RB_TILE;
+                for (int ks = 0; ks < nks; ks += RSTAGE_K) {
+                    const uint32_t n = ks + RSTAGE_K <= nks ? RSTAGE_K : (uint32_t)(nks - ks);
+                    if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, status, RSTATUS << 0)) { ok = false; break; }
+                    mbar_expect_tx(full0 + 8 * stage, n * (RA_TILE + RB_TILE));
+                    bulk_g2s(smem_u32(stA + stage * RSTAGE_A), srcA + (size_t)ks * RA_TILE, n * RA_TILE,
+                             full0 + 8 * stage);
+                    bulk_g2s(smem_u32(stB + stage * RSTAGE_B), srcB + (size_t)ks * RB_TILE, n * RB_TILE,
+                             full0 + 8 * stage);
+                    armed[stage] = 1 + phase;
+                    if (++stage == RNSTAGE) { stage = 0; phase ^= 1; }
+                }
+            }
+            // every armed stage's copies land before the CTA exits
+            for (int i = 0; i < RNSTAGE; i++)
+                if (armed[i]) mbar_wait(full0 + 8 * i, armed[i] - 1, status, RSTATUS << 1);
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            // K-direction core-matrix stride (LBO) 128 B, row-group stride (SBO) 256 B
+            const uint64_t a0 = sdesc(smem_u32(stA), 128, 256), b0 = sdesc(smem_u32(stB), 128, 256);
+            const uint32_t idesc = idesc_bf16(TM, RTN);
+            int stage = 0;
+            uint32_t phase = 0, uc = 0;
+            bool ok = true;
+            for (int64_t u = blockIdx.x; u < total && ok; u += gridDim.x, uc++) {
+                const uint32_t acc = uc & 1;
+                if (!mbar_wait(tempty0 + 8 * acc, ((uc >> 1) & 1) ^ 1, status, RSTATUS << 2)) { ok = false; break; }
+                tc_fence_after();
+                const uint32_t dt = tmem + acc * RTN;
+                for (int ks = 0; ks < nks; ks += RSTAGE_K) {
+                    const int n = ks + RSTAGE_K <= nks ? RSTAGE_K : nks - ks;
+                    if (!mbar_wait(full0 + 8 * stage, phase, status, RSTATUS << 3)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint64_t sa = (uint64_t)((uint32_t)stage * RSTAGE_A) >> 4;
+                    const uint64_t sb = (uint64_t)((uint32_t)stage * RSTAGE_B) >> 4;
+#pragma unroll
+                    for (int j = 0; j < RSTAGE_K; j++)
+                        if (j < n)
+                            umma(dt, a0 + sa + (uint64_t)(j * RA_TILE >> 4), b0 + sb + (uint64_t)(j * RB_TILE >> 4),
+                                 idesc, (ks + j) > 0 ? 1u : 0u);
+                    umma_commit(empty0 + 8 * stage);
+                    if (++stage == RNSTAGE) { stage = 0; phase ^= 1; }
+                }
+                if (!ok) break;
+                umma_commit(tfull0 + 8 * acc);
+            }
+            // every issued MMA completes before TMEM is released
+            umma_commit(finalb);
+            mbar_wait(finalb, 0, status, RSTATUS << 4);
+        }
+    } else {
+        // ------------------------------------------------ epilogue (8 warps)
+        const int quarter = warp & 3;          // TMEM lanes 32*quarter.. (rows of the tile)
+        const int colhalf = (warp - 2) >> 2;   // columns 128*colhalf.. of the accumulator
+        uint32_t uc = 0;
+        for (int64_t u = blockIdx.x; u < total; u += gridDim.x, uc++) {
+            const int leafi = (int)(u / per_leaf);
+            const int64_t rem = u % per_leaf;
+            const int l = (int)(rem / tiles);
+            const int64_t tile = rem % tiles;
+            const int mt = (int)(tile / g.rtiles), rt = (int)(tile % g.rtiles);
+            const uint32_t acc = uc & 1;
+            // warp-uniform: tcgen05.ld below is .sync.aligned
+            const bool got = mbar_wait(tfull0 + 8 * acc, (uc >> 1) & 1, status, RSTATUS << 5);
+            if (!__all_sync(0xffffffffu, got)) break;
+            tc_fence_after();
+            const float p = c_crt.p[l], invp = c_crt.invp[l], y = c_crt.y[L - 1][l];
+            unsigned char *out = (unsigned char *)leaf_digits(ws, g, leafi) + g.off_ro +
+                                 ((((size_t)l * g.mtiles + mt) * g.rtiles + rt) * RTN) * TM + quarter * 32 + lane;
+#pragma unroll 1
+            for (int c4 = 0; c4 < 4; c4++) {
+                uint32_t v[32];
+                const int col0 = colhalf * 128 + c4 * 32;
+                tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + acc * RTN + col0, v);
+#pragma unroll
+                for (int e = 0; e < 32; e++) {
+                    // c = sum rA rB (exact, |c| < 2^24).  q = c / p rounded by
+                    // MAGIC is floor or ceil of c / p (|c / p| 2^-24 < 1/2 away),
+                    // so c - q p lies in [-p, p) and one correction gives
+                    // r = c mod p in [0, p).
+                    const float c = __uint_as_float(v[e]);
+                    float r = fmaf(-(fmaf(c, invp, MAGIC) - MAGIC), p, c);
+                    r = r < 0.0f ? r + p : r;
+                    // z = r y mod p, the same way (r y < 2^15, exact)
+                    const float ry = r * y;
+                    float z = fmaf(-(fmaf(ry, invp, MAGIC) - MAGIC), p, ry);
+                    z = z < 0.0f ? z + p : z;
+                    out[(size_t)(col0 + e) * TM] = (unsigned char)__float_as_uint(z + MAGIC);  // low byte: z
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty0 + 8 * acc);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+    }
+}
+
+// ---------------------------------------------------------------- combine
+namespace {
+
+// The encoding of the double nearest |v| 2^e (ties to even), with the sign
+// of v, for |v| = hi 2^64 + lo < 2^127.  One rounding: the integer is rounded
+// at the result's last place -- 53 significant bits, or 2^-1074 for a
+// subnormal result -- and the encoding is then assembled with integer
+// operations (the FP64 pipe runs at 1/64 of FP32 here): for a significand
+// m <= 2^53 whose last place is 2^ex, the bits are ((ex + 1074) << 52) + m,
+// which also covers subnormals (ex = -1074, m < 2^52) and a rounding carry
+// into the exponent.
+__device__ __forceinline__ unsigned long long round_scaled_bits(uint64_t hi, uint64_t lo, bool neg, int e) {
+    if ((hi | lo) == 0) return 0;
+    const int nb = hi ? 128 - __clzll((long long)hi) : 64 - __clzll((long long)lo);
+    int ex = nb - 53 + e;
+    if (ex < -1074) ex = -1074;
+    const int s = ex - e;  // right shift of |v| that leaves the significand
+    uint64_t mant;
+    if (s <= 0) {
+        mant = lo << (-s);  // |v| < 2^53 here
+    } else if (s >= 128) {
+        mant = 0;           // below half of 2^-1074
+    } else {
+        uint64_t q, rb, st;
+        if (s < 64) {
+            q = (lo >> s) | (hi << (64 - s));
+            rb = (lo >> (s - 1)) & 1;
+            st = lo & ((1ull << (s - 1)) - 1);
+        } else if (s == 64) {
+            q = hi;
+            rb = lo >> 63;
+            st = lo << 1;
+        } else {
+            q = hi >> (s - 64);
+            rb = (hi >> (s - 65)) & 1;
+            st = (hi & ((1ull << (s - 65)) - 1)) | lo;
+        }
+        mant = q + (rb & ((st != 0) | (q & 1)));
+    }
+    const unsigned long long sign = neg ? 0x8000000000000000ull : 0ull;
+    if (ex > 971) return sign | 0x7FF0000000000000ull;  // |result| >= 2^1024
+    return sign | (((unsigned long long)(ex + 1074) << 52) + mant);
+}
+
+}  // namespace
+
+// One thread = 4 consecutive rows of one column of one leaf; a warp = the
+// 128 rows of a tile column, so each residue plane is read as 128
+// consecutive bytes and C written as 1 KiB.
+__global__ void __launch_bounds__(256) crt_combine_kernel(const LeafTask *__restrict__ tasks,
+                                                          char *__restrict__ ws, Geo g) {
+    const SplitHdr *h = reinterpret_cast<const SplitHdr *>(ws);
+    if (!h->residues) return;
+    const int L = h->moduli;
+    const int leafi = blockIdx.y;
+    const int64_t M = g.m;
+    const int64_t colblocks = (M + 7) / 8;
+    const int mt = (int)(blockIdx.x / colblocks);
+    const int64_t j = (blockIdx.x % colblocks) * 8 + (threadIdx.x >> 5);
+    if (mt >= g.mtiles || j >= M) return;
+    const int r0 = (threadIdx.x & 31) * 4;  // row within the tile
+    const int64_t i0 = (int64_t)mt * TM + r0;
+    if (i0 >= M) return;
+    const int rt = (int)(j / RTN), col = (int)(j % RTN);
+    const char *pl = leaf_digits(ws, g, leafi);
+    const char *sc = leaf_scalars(ws, g, leafi);
+    const size_t plane = (size_t)g.mtiles * g.rtiles * RTN * TM;
+    const uint32_t *res = reinterpret_cast<const uint32_t *>(
+        pl + g.off_ro + (((size_t)mt * g.rtiles + rt) * RTN + col) * TM + r0);
+
+    // all residue loads in flight at once: 4 rows of this column per modulus
+    uint32_t zq[LMAX];
+#pragma unroll
+    for (int l = 0; l < LMAX; l++) zq[l] = l < L ? __ldg(res + l * (plane / 4)) : 0u;
+    // S = sum_l z_l (M_L / p_l), in 32-bit limbs with 64-bit column sums
+    uint64_t s[4][4];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) s[q][k] = 0;
+#pragma unroll
+    for (int l = 0; l < LMAX; l++) {
+        if (l < L) {
+            const uint32_t *ml = c_crt.Ml[L - 1][l];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const uint32_t z = (zq[l] >> (8 * q)) & 255u;
+#pragma unroll
+                for (int k = 0; k < 4; k++) s[q][k] += (uint64_t)z * ml[k];
+            }
+        }
+    }
+    const uint64_t Mlo = (uint64_t)c_crt.M[L - 1][0] | ((uint64_t)c_crt.M[L - 1][1] << 32);
+    const uint64_t Mhi = (uint64_t)c_crt.M[L - 1][2] | ((uint64_t)c_crt.M[L - 1][3] << 32);
+    const u128 Mv = ((u128)Mhi << 64) | Mlo;
+    const u128 Mhalf = Mv >> 1;
+    const float minv = c_crt.m_inv[L - 1];
+
+    const int ej = reinterpret_cast<const int *>(sc + g.off_eb)[j];
+    double *C = tasks[leafi].C;
+    unsigned long long outb[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int64_t i = i0 + q;
+        // carry the column sums into a 128-bit S < L M_L < 2^128
+        uint64_t c = s[q][0];
+        const uint32_t w0 = (uint32_t)c;
+        c = s[q][1] + (c >> 32);
+        const uint32_t w1 = (uint32_t)c;
+        c = s[q][2] + (c >> 32);
+        const uint32_t w2 = (uint32_t)c;
+        c = s[q][3] + (c >> 32);
+        const uint64_t Slo = ((uint64_t)w1 << 32) | w0, Shi = (c << 32) | w2;
+        const u128 S = ((u128)Shi << 64) | Slo;
+        // S mod M_L: the fp32 quotient is within 1 of floor(S / M_L) (<= 16)
+        const float sf = fmaf((float)Shi, 18446744073709551616.0f, (float)Slo);
+        int qe = (int)(sf * minv);
+        qe = qe < 0 ? 0 : qe;
+        u128 qm = (u128)(uint32_t)qe * Mv;
+        if (qm > S) qm -= Mv;
+        u128 Cr = S - qm;
+        if (Cr >= Mv) Cr -= Mv;
+        // centre: C' in (-M/2, M/2)
+        const bool neg = Cr > Mhalf;
+        const u128 mag = neg ? Mv - Cr : Cr;
+        const int ei = i < M ? reinterpret_cast<const int *>(sc + g.off_ea)[i] : 0;
+        // C = C' 2^(E_i + E_j - ta - tb); a zero row / column has C' = 0
+        if (ei != 0 && ej != 0)
+            outb[q] = round_scaled_bits((uint64_t)(mag >> 64), (uint64_t)mag, neg,
+                                        (ei - 4096) + (ej - 4096) - h->ta - h->tb);
+    }
+    if (i0 + 3 < M && ((uintptr_t)(C + i0 + j * M) & 15) == 0) {
+        double2 *dst = reinterpret_cast<double2 *>(C + i0 + j * M);
+        dst[0] = make_double2(__longlong_as_double((long long)outb[0]), __longlong_as_double((long long)outb[1]));
+        dst[1] = make_double2(__longlong_as_double((long long)outb[2]), __longlong_as_double((long long)outb[3]));
+    } else {
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (i0 + q < M) C[i0 + q + j * M] = __longlong_as_double((long long)outb[q]);
+    }
+}
+
+// ---------------------------------------------------------------- launchers
+static CrtTables g_tables_host;
+static bool g_tables_built = false;
+static int g_crt_device = -1;
+static cudaError_t g_crt_error = cudaSuccess;
+
+cudaError_t crt_prepare() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (g_crt_device == dev) return g_crt_error;
+    if (!g_tables_built) {
+        build_tables(g_tables_host);
+        g_tables_built = true;
+    }
+    g_crt_error = cudaMemcpyToSymbol(c_crt, &g_tables_host, sizeof(CrtTables));
+    if (g_crt_error == cudaSuccess) {
+        const size_t smem = (size_t)RNSTAGE * RSTAGE_BYTES + 1024 + 1024;
+        g_crt_error = cudaFuncSetAttribute(crt_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
+    g_crt_device = dev;
+    return g_crt_error;
+}
+
+cudaError_t launch_crt_resolve(int count, int m, SplitParams p, void *workspace, cudaStream_t stream) {
+    Geo g = make_geo(m, count, p.scheme);
+    crt_resolve_kernel<<<1, 32, 0, stream>>>((char *)workspace, g, p);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_crt_slice(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
+                             cudaStream_t stream) {
+    Geo g = make_geo(m, count, p.scheme);
+    if (!g.residues_ok) return cudaSuccess;
+    const int64_t atiles = (int64_t)g.mtiles * g.nks, bhalves = (int64_t)g.rtiles * g.nks * 2;
+    dim3 grid((unsigned)(atiles > bhalves ? atiles : bhalves), 2, (unsigned)count);
+    crt_slice_kernel<<<grid, 256, 0, stream>>>(tasks_dev, (char *)workspace, g);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_crt_gemm(const LeafTask *, int count, int m, SplitParams p, void *workspace,
+                            unsigned int *status_dev, int num_sms, cudaStream_t stream) {
+    Geo g = make_geo(m, count, p.scheme);
+    if (!g.residues_ok) return cudaSuccess;
+    cudaError_t e = crt_prepare();
+    if (e != cudaSuccess) return e;
+    const int64_t most = (int64_t)g.mtiles * g.rtiles * LMAX * count;  // units, at the most moduli
+    const int grid = (int)(most < num_sms ? most : num_sms);
+    const size_t smem = (size_t)RNSTAGE * RSTAGE_BYTES + 1024 + 1024;
+    crt_gemm_kernel<<<grid, RGEMM_THREADS, smem, stream>>>((char *)workspace, g, status_dev);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split_combine(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
+                                 cudaStream_t stream) {
+    Geo g = make_geo(m, count, p.scheme);
+    if (!g.residues_ok) return cudaSuccess;
+    const int64_t colblocks = (m + 7) / 8;
+    dim3 grid((unsigned)(g.mtiles * colblocks), (unsigned)count);
+    crt_combine_kernel<<<grid, 256, 0, stream>>>(tasks_dev, (char *)workspace, g);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace caps

@@ -36,16 +36,14 @@
 // All mbarrier waits are bounded; a wait that gives up sets a bit in the
 // status word the host reads back (CAPS_ERR_TIMEOUT) and the kernel unwinds,
 // waiting (bounded) for its own copies and MMAs before freeing TMEM.
-#include "common.cuh"
+#include "split_common.cuh"
 
 namespace caps {
 
+using namespace split;
+
 namespace {
 
-constexpr int TM = 128;         // rows of A per tile (TMEM lanes)
-constexpr int TN = 64;          // columns of B per tile (per diagonal region)
-constexpr int TK = 16;          // K per MMA / per pipeline stage
-constexpr int MAXS = 8;         // max digits
 constexpr int CHUNK = 32;       // K16 steps per exact accumulation chunk (K = 512)
 constexpr int SUB = 2;           // 16-deep K steps per pipeline stage (K = 32 per stage)
 constexpr int NSTAGE = 2;
@@ -55,92 +53,11 @@ constexpr int STAGE_A = SUB * MAXS * A_PLANE_BYTES;
 constexpr int STAGE_B = SUB * MAXS * B_PLANE_BYTES;
 constexpr int STAGE_BYTES = STAGE_A + STAGE_B;  // 96 KiB
 constexpr int GEMM_THREADS = 320;               // producer, MMA, 8 epilogue warps
-constexpr uint32_t WAIT_LIMIT = 1u << 25;
-
-struct SplitHdr {
-    int needed;   // max digits needed over the group
-    int s_used;   // written by the gemm for the host
-    int nd_used;
-    int pad[61];
-};
-
-// Workspace of one launch group of `count` leaves:
-//   [header 256 B][scalars of leaf 0..count-1][digit planes of leaf 0..count-1]
-// scalars per leaf: f (A rows), g (B columns), and the scan's exponent / lsb
-// encodings; digits per leaf: A planes then B planes, pre-tiled.
-struct Geo {
-    int m, Mp, Np, Kp, nks, mtiles, ntiles, count;
-    size_t sc_per_leaf, dg_per_leaf, sc_base, dg_base, total;
-    size_t off_fa, off_fb, off_ea, off_la, off_eb, off_lb;  // within a scalar block
-    size_t off_da, off_db;                                  // within a digit block
-};
-
-__host__ __device__ inline Geo make_geo(int m, int count) {
-    Geo g;
-    g.m = m;
-    g.count = count;
-    g.Mp = (m + TM - 1) / TM * TM;
-    g.Np = (m + TN - 1) / TN * TN;
-    g.Kp = (m + TK - 1) / TK * TK;
-    g.nks = g.Kp / TK;
-    g.mtiles = g.Mp / TM;
-    g.ntiles = g.Np / TN;
-    size_t o = 0;
-    g.off_fa = o; o += ((size_t)g.Mp * 4 + 255) & ~(size_t)255;
-    g.off_fb = o; o += ((size_t)g.Np * 4 + 255) & ~(size_t)255;
-    g.off_ea = o; o += ((size_t)g.Mp * 4 + 255) & ~(size_t)255;
-    g.off_la = o; o += ((size_t)g.Mp * 4 + 255) & ~(size_t)255;
-    g.off_eb = o; o += ((size_t)g.Np * 4 + 255) & ~(size_t)255;
-    g.off_lb = o; o += ((size_t)g.Np * 4 + 255) & ~(size_t)255;
-    g.sc_per_leaf = o;
-    o = 0;
-    g.off_da = o; o += ((size_t)g.Mp * g.Kp * 2 * MAXS + 255) & ~(size_t)255;
-    g.off_db = o; o += ((size_t)g.Np * g.Kp * 2 * MAXS + 255) & ~(size_t)255;
-    g.dg_per_leaf = o;
-    g.sc_base = 256;
-    g.dg_base = 256 + (size_t)count * g.sc_per_leaf;
-    g.total = g.dg_base + (size_t)count * g.dg_per_leaf;
-    return g;
-}
-
-__device__ __forceinline__ char *leaf_scalars(char *ws, const Geo &g, int l) {
-    return ws + g.sc_base + (size_t)l * g.sc_per_leaf;
-}
-__device__ __forceinline__ char *leaf_digits(char *ws, const Geo &g, int l) {
-    return ws + g.dg_base + (size_t)l * g.dg_per_leaf;
-}
-
-__device__ __forceinline__ void resolve_sd(const SplitHdr *h, SplitParams p, int &s, int &nd) {
-    int need = h->needed;
-    if (need < 1) need = 1;
-    if (need > MAXS) need = MAXS;
-    s = p.slices > 0 ? p.slices : need;
-    if (s > MAXS) s = MAXS;
-    nd = p.diagonals > 0 ? p.diagonals : (2 * s - 1 < 8 ? 2 * s - 1 : 8);
-    if (nd > 2 * s - 1) nd = 2 * s - 1;  // no digit pair lies beyond diagonal 2s
-    if (nd > 8) nd = 8;
-    if (nd < 1) nd = 1;
-}
-
-// exponent bound E (|x| < 2^E) and lowest set bit of x != 0
-__device__ __forceinline__ void exp_lsb(double x, int &E, int &lsb) {
-    unsigned long long u = (unsigned long long)__double_as_longlong(x);
-    int field = (int)((u >> 52) & 0x7ff);
-    unsigned long long mant = u & 0xFFFFFFFFFFFFFull;
-    if (field == 0) {
-        E = -1022;
-        lsb = -1074 + (__ffsll((long long)mant) - 1);
-    } else {
-        E = field - 1022;
-        unsigned long long M = mant | (1ull << 52);
-        lsb = field - 1075 + (__ffsll((long long)M) - 1);
-    }
-}
 
 }  // namespace
 
-size_t split_workspace_bytes(int m, int count, int /*slices*/) {
-    return make_geo(m, count).total;
+size_t split_workspace_bytes(int m, int count, int scheme) {
+    return make_geo(m, count, scheme).total;
 }
 
 // ---------------------------------------------------------------- scan
@@ -203,12 +120,13 @@ __global__ void __launch_bounds__(256) split_scan_kernel(const LeafTask *__restr
     }
 }
 
-// f = 55 - E per row / column; digits needed (max over the group)
+// f = 55 - E per row / column (digit scheme); digits needed, and the bits
+// E - lsb + 1 per side (max over the group) for the scheme choice
 __global__ void __launch_bounds__(256) split_finalize_kernel(char *__restrict__ ws, Geo g) {
     char *leaf = leaf_scalars(ws, g, blockIdx.y);
     SplitHdr *h = reinterpret_cast<SplitHdr *>(ws);
     int idx = blockIdx.x * 256 + threadIdx.x;
-    int need = 0;
+    int need = 0, bits[2] = {0, 0};
     if (idx < g.m) {
         for (int side = 0; side < 2; side++) {
             int ee = reinterpret_cast<int *>(leaf + (side ? g.off_eb : g.off_ea))[idx];
@@ -217,52 +135,28 @@ __global__ void __launch_bounds__(256) split_finalize_kernel(char *__restrict__ 
             if (ee != 0) {
                 int E = ee - 4096, lsb = 4096 - le;
                 f = 55 - E;
-                int bits = E - lsb + 1;
-                int s = (bits + 6) / 7;
+                int b = E - lsb + 1;
+                int s = (b + 6) / 7;
                 need = s > need ? s : need;
+                bits[side] = b;
             }
             reinterpret_cast<int *>(leaf + (side ? g.off_fb : g.off_fa))[idx] = f;
         }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) need = max(need, __shfl_xor_sync(0xffffffffu, need, o));
-    if ((threadIdx.x & 31) == 0 && need > 0) atomicMax(&h->needed, need);
+    for (int o = 16; o > 0; o >>= 1) {
+        need = max(need, __shfl_xor_sync(0xffffffffu, need, o));
+        bits[0] = max(bits[0], __shfl_xor_sync(0xffffffffu, bits[0], o));
+        bits[1] = max(bits[1], __shfl_xor_sync(0xffffffffu, bits[1], o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (need > 0) atomicMax(&h->needed, need);
+        if (bits[0] > 0) atomicMax(&h->bitsA, bits[0]);
+        if (bits[1] > 0) atomicMax(&h->bitsB, bits[1]);
+    }
 }
 
 // ---------------------------------------------------------------- slice
-// round(x 2^f) to nearest, ties to even, for |x 2^f| <= 2^55, by integer
-// operations on the IEEE bits (the FP64 pipe runs at 1/64 of FP32 here).
-// With x = +-M 2^e (M < 2^53) and f = 55 - E, E >= e + 53, the shift e + f
-// is at most 3, so a left shift never overflows.
-__device__ __forceinline__ long long scaled_round(double x, int f) {
-    unsigned long long u = (unsigned long long)__double_as_longlong(x);
-    int field = (int)((u >> 52) & 0x7ff);
-    unsigned long long M = u & 0xFFFFFFFFFFFFFull;
-    int e;
-    if (field == 0) {
-        if (M == 0) return 0;
-        e = -1074;
-    } else {
-        M |= 1ull << 52;
-        e = field - 1075;
-    }
-    int sh = e + f;
-    unsigned long long q;
-    if (sh >= 0) {
-        q = M << sh;
-    } else {
-        int r = -sh;
-        if (r > 63) {
-            q = 0;
-        } else {
-            q = M >> r;
-            unsigned long long rem = M & ((1ull << r) - 1), half = 1ull << (r - 1);
-            if (rem > half || (rem == half && (q & 1))) q++;
-        }
-    }
-    return (u >> 63) ? -(long long)q : (long long)q;
-}
-
 // balanced base-128 digits of round(x 2^f), most significant first.
 // X + 64 (1 + 128 + ... + 128^7) has ordinary base-128 digits d_k + 64, so
 // each balanced digit is a 7-bit field minus 64; the top field is not masked
@@ -293,6 +187,7 @@ __device__ __forceinline__ uint32_t bf16_of_digit(int d) {
 // 64 x 16 tiles.
 __global__ void __launch_bounds__(256) split_slice_kernel(const LeafTask *__restrict__ tasks, int m,
                                                           char *__restrict__ ws, Geo g, SplitParams p) {
+    if (reinterpret_cast<const SplitHdr *>(ws)->residues) return;  // the residue scheme runs
     const LeafTask t = tasks[blockIdx.z];
     char *sc = leaf_scalars(ws, g, blockIdx.z);
     char *dg = leaf_digits(ws, g, blockIdx.z);
@@ -364,111 +259,6 @@ __global__ void __launch_bounds__(256) split_slice_kernel(const LeafTask *__rest
 // ---------------------------------------------------------------- gemm
 namespace {
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// bounded wait: false (and a status bit) if the phase never completes
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned *status,
-                                          unsigned code) {
-    for (uint32_t it = 0; it < WAIT_LIMIT; it++) {
-        if (mbar_try(bar, parity)) return true;
-        if (it > 64) __nanosleep(it > 4096 ? 256 : 32);
-    }
-    atomicOr(status, code);
-    return false;
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes,
-                                         uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            dst),
-        "l"(src), "r"(bytes), "r"(bar)
-        : "memory");
-}
-
-// UMMA shared-memory descriptor, K-major, no swizzle.
-__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-    uint64_t d = 0;
-    d |= (uint64_t)((addr >> 4) & 0x3FFF);
-    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
-    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
-    d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
-    return d;                // base offset 0, swizzle none
-}
-
-// instruction descriptor: kind::f16, A=B=bf16, D=f32, K-major, M x N
-__device__ __forceinline__ uint32_t idesc_bf16(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
-           ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void umma(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc,
-                                     uint32_t acc) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
-        "l"(a), "l"(b), "r"(idesc), "r"(acc));
-}
-
-__device__ __forceinline__ void umma_commit(uint32_t bar) {
-    asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-        : "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() {
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-          "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
-          "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
-          "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
-}  // namespace
-
-namespace {
-
 // The MMA sequence of one 16-deep K step depends only on (s, nd) and on the
 // stage: it is built once per CTA (stage 0 addresses), kept in registers, and
 // each step adds the stage offset to the descriptors' address fields.
@@ -526,14 +316,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * NSTAGE + 3);
     MmaTable *mtab = reinterpret_cast<MmaTable *>(bars + 16);
 
+    if (reinterpret_cast<const SplitHdr *>(ws)->residues) return;  // the residue scheme runs
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int s, nd;
     resolve_sd(reinterpret_cast<const SplitHdr *>(ws), p, s, nd);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        SplitHdr *h = reinterpret_cast<SplitHdr *>(ws);
-        h->s_used = s;
-        h->nd_used = nd;
-    }
     const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + NSTAGE);
     const uint32_t tfull = smem_u32(bars + 2 * NSTAGE), tempty = smem_u32(bars + 2 * NSTAGE + 1);
     const uint32_t finalb = smem_u32(bars + 2 * NSTAGE + 2);
@@ -731,12 +517,13 @@ void split_gemm_prepare() {
     if (g_num_sms <= 0) g_num_sms = 152;
     const size_t smem = (size_t)NSTAGE * STAGE_BYTES + 1024 + 1024;
     g_prepare_error = cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (g_prepare_error == cudaSuccess) g_prepare_error = crt_prepare();
     g_prepared_device = dev;
 }
 
-cudaError_t launch_split_scan(const LeafTask *tasks_dev, int count, int m, void *workspace,
+cudaError_t launch_split_scan(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
                               cudaStream_t stream) {
-    Geo g = make_geo(m, count);
+    Geo g = make_geo(m, count, p.scheme);
     cudaError_t e = cudaMemsetAsync(workspace, 0, g.dg_base, stream);
     if (e != cudaSuccess) return e;
     int64_t ablocks = ((int64_t)(m + 255) / 256) * ((m + 255) / 256);
@@ -755,13 +542,19 @@ cudaError_t launch_split_scan(const LeafTask *tasks_dev, int count, int m, void 
 
 cudaError_t launch_split_prep(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
                               cudaStream_t stream) {
-    Geo g = make_geo(m, count);
+    Geo g = make_geo(m, count, p.scheme);
     char *ws = (char *)workspace;
     {
         dim3 grid((unsigned)((m + 255) / 256), (unsigned)count);
         split_finalize_kernel<<<grid, 256, 0, stream>>>(ws, g);
         count_launch();
     }
+    // the scheme, written into the header; of the two slicers below, the one
+    // for the other scheme returns at once
+    cudaError_t e = launch_crt_resolve(count, m, p, ws, stream);
+    if (e != cudaSuccess) return e;
+    e = launch_crt_slice(tasks_dev, count, m, p, ws, stream);
+    if (e != cudaSuccess) return e;
     {
         int64_t atiles = (int64_t)g.mtiles * g.nks;
         int64_t btiles2 = ((int64_t)g.ntiles * g.nks + 1) / 2;
@@ -775,7 +568,7 @@ cudaError_t launch_split_prep(const LeafTask *tasks_dev, int count, int m, Split
 
 cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
                               unsigned int *status_dev, cudaStream_t stream) {
-    Geo g = make_geo(m, count);
+    Geo g = make_geo(m, count, p.scheme);
     char *ws = (char *)workspace;
     cudaError_t e;
     split_gemm_prepare();
@@ -786,7 +579,9 @@ cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, Split
     int grid = (int)(total < g_num_sms ? total : g_num_sms);
     split_gemm_kernel<<<grid, GEMM_THREADS, smem, stream>>>(tasks_dev, count, ws, g, p, status_dev);
     count_launch();
-    return cudaGetLastError();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_crt_gemm(tasks_dev, count, m, p, ws, status_dev, g_num_sms, stream);
 }
 
 cudaError_t split_needed_slices(void *workspace, int, int, int *needed, cudaStream_t stream) {

@@ -87,7 +87,7 @@ extern "C" caps_status caps_leaf_gemm_split_noalloc_dev(const double *A, const d
         caps::set_last_error_text("m exceeds the no-allocation scratch limit of 512");
         return CAPS_ERR_SIZE;
     }
-    size_t need = caps::split_workspace_bytes(m, 1, 8);
+    size_t need = caps::split_workspace_bytes(m, 1, CAPS_SPLIT_DIGITS);
     if (need > TASK_OFF) {
         caps::set_last_error_text("split workspace exceeds the no-allocation scratch array");
         return CAPS_ERR_SIZE;
@@ -102,12 +102,13 @@ extern "C" caps_status caps_leaf_gemm_split_noalloc_dev(const double *A, const d
     caps::SplitParams p;
     p.slices = slices;
     p.diagonals = diagonals;
+    p.scheme = CAPS_SPLIT_DIGITS;  // the scratch array is sized for digit planes
 
     noalloc_set_task<<<1, 1, 0, s>>>(task, A, B, C);
     caps::count_launch();
     CAPS_CUDA_TRY(cudaGetLastError());
     CAPS_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(unsigned), s));
-    CAPS_CUDA_TRY(caps::launch_split_scan(task, 1, m, ws, s));   // clears header and scales
+    CAPS_CUDA_TRY(caps::launch_split_scan(task, 1, m, p, ws, s));   // clears header and scales
     CAPS_CUDA_TRY(caps::launch_split_prep(task, 1, m, p, ws, s));
     CAPS_CUDA_TRY(caps::launch_split_gemm(task, 1, m, p, ws, status, s));
     unsigned h = 0;

@@ -51,11 +51,24 @@ typedef enum caps_form {
                             integer slice products on tcgen05, FP64 recombine */
 } caps_form;
 
+/* How the split form cuts the base-case operands.  Both scale each row of A
+ * and column of B by a power of two into integers of up to 55 bits. */
+typedef enum caps_split_scheme {
+    CAPS_SPLIT_AUTO = 0,     /* per launch group of leaves, from the data: residues
+                                when they need fewer tensor-core products (float
+                                data), digits otherwise (integer-like data) */
+    CAPS_SPLIT_DIGITS = 1,   /* balanced base-128 digits, one product per kept
+                                digit pair (36 for float data) */
+    CAPS_SPLIT_RESIDUES = 2  /* residues modulo up to 17 coprime moduli <= 181,
+                                one product per modulus, exact CRT recombination;
+                                leaves up to 2048 (larger leaves use digits) */
+} caps_split_scheme;
+
 typedef struct caps_options {
     int form;                  /* caps_form */
     int slices;                /* split form: digits per operand, 0 = automatic, 1..8 */
     int diagonals;             /* split form: digit-pair diagonals kept, 0 = automatic */
-    int reserved0;
+    int split_scheme;          /* split form: caps_split_scheme */
     long long workspace_limit; /* bytes of device workspace allowed (-m); <= 0: no limit */
     long long reserved[4];
 } caps_options;
@@ -135,6 +148,8 @@ typedef struct caps_counters {
     long long leaf_gemm_launches;
     double leaf_gemm_m3;     /* sum of leaves * m^3 over those launches */
     long long add_bytes;     /* algorithmic bytes read + written by the sum / combination kernels */
+    int split_moduli;        /* moduli used by the last split multiply's residue scheme (0: digits ran) */
+    int split_pad;
 } caps_counters;
 
 void caps_get_counters(caps_counters *out);

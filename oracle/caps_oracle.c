@@ -465,3 +465,108 @@ void caps_oracle_split_gemm(int64_t m, const double *A, const double *B, int s, 
     }
     free(da); free(db); free(fa); free(fb);
 }
+
+/* ---------------------------------------------------------------------- */
+/* CPU model of the residue scheme of the split base case.                 */
+/* Not a reference algorithm either.  The GPU computes the product of the  */
+/* scaled integers exactly through residues modulo small coprime moduli;   */
+/* the model computes the same integer product directly in 128-bit         */
+/* integers, independent of the moduli, and rounds it the same way.        */
+/*                                                                         */
+/* Per row i of A: E_i = max exponent bound, lsb_i = min lowest set bit;   */
+/* t_a = min(max_i (E_i - lsb_i + 1), 55), fa_i = t_a - E_i, and           */
+/* X_ik = round-half-even(a_ik 2^fa_i); the same per column of B.          */
+/* C_ij = sum_k X_ik Y_kj (exact) times 2^-(fa_i + fb_j), rounded once to   */
+/* the nearest double (ties to even, subnormals included).                 */
+/* ---------------------------------------------------------------------- */
+
+/* exponent of the lowest set bit of x != 0 */
+static int low_bit(double x)
+{
+    uint64_t u;
+    memcpy(&u, &x, 8);
+    int field = (int)((u >> 52) & 0x7ff);
+    uint64_t mant = u & 0xFFFFFFFFFFFFFULL;
+    if (field == 0) return -1074 + __builtin_ctzll(mant);
+    return field - 1075 + __builtin_ctzll(mant | (1ULL << 52));
+}
+
+/* |v| 2^e rounded to the nearest double (ties to even), signed */
+static double round_scaled_i128(__int128 v, int e)
+{
+    if (v == 0) return 0.0;
+    int neg = v < 0;
+    unsigned __int128 mag = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
+    int nb = 0;
+    while (nb < 128 && (mag >> nb) != 0) nb++;
+    int sh = nb - 53;
+    if (nb - 1 + e < -1022) sh = -1074 - e;
+    uint64_t mant;
+    int ex;
+    if (sh <= 0) {
+        mant = (uint64_t)mag;
+        ex = e;
+    } else if (sh >= 128) {
+        mant = 0;
+        ex = e;
+    } else {
+        unsigned __int128 q = mag >> sh, rem = mag - (q << sh), half = (unsigned __int128)1 << (sh - 1);
+        mant = (uint64_t)q;
+        if (rem > half || (rem == half && (mant & 1))) mant++;
+        ex = e + sh;
+    }
+    double r = ldexp((double)mant, ex);
+    return neg ? -r : r;
+}
+
+/* scale exponents of the rows of a column-major m x m matrix taken as rows
+ * (side 0: rows of A, element (i,k) at i + k m) or as columns (side 1:
+ * columns of B, element (k,j) at k + j m); returns max bits over the lines */
+static int residue_scales(int64_t m, const double *X, int side, int *E)
+{
+    int bits = 0;
+    for (int64_t r = 0; r < m; r++) {
+        int e = -100000, lb = 100000;
+        for (int64_t k = 0; k < m; k++) {
+            double x = side == 0 ? X[r + k * m] : X[k + r * m];
+            if (x == 0.0) continue;
+            int eb = exp_bound(x), l = low_bit(x);
+            if (eb > e) e = eb;
+            if (l < lb) lb = l;
+        }
+        E[r] = e;
+        if (e != -100000 && e - lb + 1 > bits) bits = e - lb + 1;
+    }
+    return bits;
+}
+
+void caps_oracle_split_gemm_residues(int64_t m, const double *A, const double *B, double *C, int *t_out)
+{
+    int *Ea = (int *)malloc((size_t)m * sizeof(int));
+    int *Eb = (int *)malloc((size_t)m * sizeof(int));
+    int ta = residue_scales(m, A, 0, Ea), tb = residue_scales(m, B, 1, Eb);
+    if (ta > 55) ta = 55;
+    if (tb > 55) tb = 55;
+    if (t_out) { t_out[0] = ta; t_out[1] = tb; }
+    int64_t *X = (int64_t *)malloc((size_t)(m * m) * sizeof(int64_t));  /* row-major X[i][k] */
+    int64_t *Y = (int64_t *)malloc((size_t)(m * m) * sizeof(int64_t));  /* Y[j][k] */
+    for (int64_t i = 0; i < m; i++)
+        for (int64_t k = 0; k < m; k++)
+            X[i * m + k] = Ea[i] == -100000 ? 0 : (int64_t)nearbyint(ldexp(A[i + k * m], ta - Ea[i]));
+    for (int64_t j = 0; j < m; j++)
+        for (int64_t k = 0; k < m; k++)
+            Y[j * m + k] = Eb[j] == -100000 ? 0 : (int64_t)nearbyint(ldexp(B[k + j * m], tb - Eb[j]));
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t j = 0; j < m; j++) {
+        for (int64_t i = 0; i < m; i++) {
+            __int128 acc = 0;
+            const int64_t *x = X + i * m, *y = Y + j * m;
+            for (int64_t k = 0; k < m; k++) acc += (__int128)x[k] * y[k];
+            double v = 0.0;
+            if (Ea[i] != -100000 && Eb[j] != -100000)
+                v = round_scaled_i128(acc, -((ta - Ea[i]) + (tb - Eb[j])));
+            C[i + j * m] = v;
+        }
+    }
+    free(X); free(Y); free(Ea); free(Eb);
+}

@@ -74,6 +74,8 @@ def lib():
         L.caps_oracle_split_gemm.argtypes = [ctypes.c_int64, _dp, _dp, ctypes.c_int,
                                              ctypes.c_int, _dp]
         L.caps_oracle_set_dgemm.restype = None
+        L.caps_oracle_split_gemm_residues.restype = None
+        L.caps_oracle_split_gemm_residues.argtypes = [ctypes.c_int64, _dp, _dp, _dp, ctypes.POINTER(ctypes.c_int)]
         L.caps_oracle_set_dgemm.argtypes = [ctypes.c_void_p]
         L.caps_oracle_set_threads.restype = None
         L.caps_oracle_set_threads.argtypes = [ctypes.c_int]
@@ -208,6 +210,17 @@ def split_gemm(A_cm: np.ndarray, B_cm: np.ndarray, m: int, s: int, nd: int) -> n
     lib().caps_oracle_split_gemm(m, _p(np.ascontiguousarray(A_cm)), _p(np.ascontiguousarray(B_cm)),
                                  int(s), int(nd), _p(C))
     return C
+
+
+def split_gemm_residues(A_cm: np.ndarray, B_cm: np.ndarray, m: int):
+    """Exact CPU model of the residue scheme's leaf product (column-major):
+    the 128-bit integer product of the scaled operands, rounded once.
+    Returns (C, (t_a, t_b))."""
+    C = np.empty(m * m, dtype=np.float64)
+    t = (ctypes.c_int * 2)()
+    lib().caps_oracle_split_gemm_residues(m, _p(np.ascontiguousarray(A_cm)), _p(np.ascontiguousarray(B_cm)),
+                                          _p(C), t)
+    return C, (t[0], t[1])
 
 
 # ---------------------------------------------------------------------------

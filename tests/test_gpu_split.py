@@ -1,9 +1,11 @@
 """GPU parity of the split (Ozaki-style, tcgen05) form, through the C ABI.
 
-The leaf kernel computes exact integer digit-pair products, so for the same
-digit count s and diagonal count nd it must equal the oracle's CPU model of
-the split arithmetic BIT FOR BIT.  Whole multiplies are bit-exact on integer
-inputs and, on float inputs, within the plain FP64 path's error."""
+Digit scheme: the leaf kernel computes exact integer digit-pair products, so
+for the same digit count s and diagonal count nd it must equal the oracle's
+CPU model of the split arithmetic BIT FOR BIT.  Residue scheme: the leaf
+product of the scaled integers is exact, so it must equal the oracle's
+128-bit model bit for bit.  Whole multiplies are bit-exact on integer inputs
+and, on float inputs, within the plain FP64 path's error."""
 import numpy as np
 import pytest
 
@@ -12,12 +14,13 @@ from helpers import caps_of, mat_of, gpu_multiply, dd_of, rel_err
 pytestmark = pytest.mark.gpu
 
 
-def _leaf(caps, cuda, A, B, s=0, nd=0):
+def _leaf(caps, cuda, A, B, s=0, nd=0, scheme="auto"):
     import torch
     m = A.shape[0]
     C = torch.full((m * m,), float("nan"), dtype=torch.float64, device=cuda)
     caps.leaf_gemm(torch.from_numpy(A.T.copy().reshape(-1)).to(cuda),
-                   torch.from_numpy(B.T.copy().reshape(-1)).to(cuda), C, m, form="split", slices=s, diagonals=nd)
+                   torch.from_numpy(B.T.copy().reshape(-1)).to(cuda), C, m, form="split", slices=s, diagonals=nd,
+                   scheme=scheme)
     torch.cuda.synchronize()
     return C.cpu().numpy().reshape(m, m).T, caps.counters()
 
@@ -27,9 +30,9 @@ def test_split_leaf_bitexact_vs_model_uniform(caps, oracle_mod, cuda, m):
     rng = np.random.default_rng(m)
     A = rng.uniform(-1, 1, (m, m))
     B = rng.uniform(-1, 1, (m, m))
-    C, cnt = _leaf(caps, cuda, A, B)
+    C, cnt = _leaf(caps, cuda, A, B, scheme="digits")
     s, nd = cnt["split_slices"], cnt["split_diagonals"]
-    assert (s, nd) == (8, 8)
+    assert (s, nd, cnt["split_moduli"]) == (8, 8, 0)
     ref = oracle_mod.split_gemm(A.T.copy().reshape(-1), B.T.copy().reshape(-1), m, s, nd).reshape(m, m).T
     assert np.array_equal(C, ref)
 
@@ -65,7 +68,7 @@ def test_split_leaf_zero_rows_and_tiny_values(caps, oracle_mod, cuda):
     A[7, 11] = 1e-300
     B = rng.uniform(-1, 1, (m, m)) * 1e-200
     B[:, 2] = 0.0
-    C, cnt = _leaf(caps, cuda, A, B)
+    C, cnt = _leaf(caps, cuda, A, B, scheme="digits")
     ref = oracle_mod.split_gemm(A.T.copy().reshape(-1), B.T.copy().reshape(-1), m, cnt["split_slices"],
                                 cnt["split_diagonals"]).reshape(m, m).T
     assert np.array_equal(C, ref)
@@ -79,8 +82,9 @@ def test_reference_known_answers_split(caps, oracle_mod, ref_tests, cuda, n):
     exact = (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64)
     for bs, r in ref_tests["params%d" % n]:
         for pat in ("d" * r, "b" * r):
-            C = gpu_multiply(caps, oracle_mod, A, B, r, bs, pat, form="split")
-            assert np.array_equal(C, exact), (n, bs, r, pat)
+            for scheme in ("digits", "residues"):
+                C = gpu_multiply(caps, oracle_mod, A, B, r, bs, pat, form="split", scheme=scheme)
+                assert np.array_equal(C, exact), (n, bs, r, pat, scheme)
 
 
 def test_config5_like_integers_bitexact(caps, oracle_mod, cuda):
@@ -90,13 +94,14 @@ def test_config5_like_integers_bitexact(caps, oracle_mod, cuda):
     A = rng.integers(-1024, 1025, (n, n)).astype(np.float64)
     B = rng.integers(-1024, 1025, (n, n)).astype(np.float64)
     exact = (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64)
-    for form in ("split", "plain"):
-        C = gpu_multiply(caps, oracle_mod, A, B, r, 1, "bbdd", form=form)
-        assert np.array_equal(C, exact), form
+    for form, scheme in (("split", "auto"), ("split", "residues"), ("plain", "auto")):
+        C = gpu_multiply(caps, oracle_mod, A, B, r, 1, "bbdd", form=form, scheme=scheme)
+        assert np.array_equal(C, exact), (form, scheme)
 
 
+@pytest.mark.parametrize("scheme", ["digits", "residues"])
 @pytest.mark.parametrize("wide", [False, True])
-def test_split_error_no_worse_than_plain(caps, oracle_mod, cuda, wide):
+def test_split_error_no_worse_than_plain(caps, oracle_mod, cuda, wide, scheme):
     n, r = 1024, 3
     rng = np.random.default_rng(33 + wide)
     A = rng.uniform(-1, 1, (n, n))
@@ -106,8 +111,113 @@ def test_split_error_no_worse_than_plain(caps, oracle_mod, cuda, wide):
         B *= 2.0 ** rng.integers(-20, 21, (n, n))
     hi, lo = dd_of(oracle_mod, A, B)
     Cp = gpu_multiply(caps, oracle_mod, A, B, r, 1, "ddb", form="plain")
-    Cs = gpu_multiply(caps, oracle_mod, A, B, r, 1, "ddb", form="split")
+    Cs = gpu_multiply(caps, oracle_mod, A, B, r, 1, "ddb", form="split", scheme=scheme)
     ew_p, nw_p = rel_err(Cp, hi, lo, A, B)
     ew_s, nw_s = rel_err(Cs, hi, lo, A, B)
     assert nw_s <= 1.25 * nw_p, (nw_s, nw_p)
     assert ew_s <= 1.25 * ew_p or ew_s < 1e-13, (ew_s, ew_p)
+
+
+# ---------------------------------------------------------------- residue scheme
+MODULI = [181, 180, 179, 173, 169, 167, 163, 161, 157, 151, 149, 139, 137, 131, 127, 121, 113]
+
+
+def expected_moduli(ta, tb, m):
+    """Fewest moduli whose product M has floor(log2 M) >= ta + tb + ceil(log2 Kp) + 1."""
+    kp = (m + 15) // 16 * 16
+    need = ta + tb + (kp - 1).bit_length() + 1
+    prod = 1
+    for L, p in enumerate(MODULI, 1):
+        prod *= p
+        if prod.bit_length() - 1 >= need:
+            return L
+    return None
+
+
+def _residue_ref(oracle_mod, A, B):
+    m = A.shape[0]
+    ref, t = oracle_mod.split_gemm_residues(A.T.copy().reshape(-1), B.T.copy().reshape(-1), m)
+    return ref.reshape(m, m).T, t
+
+
+@pytest.mark.parametrize("m", [128, 64, 14, 200, 512, 1100, 2048])
+def test_residue_leaf_bitexact_vs_model_uniform(caps, oracle_mod, cuda, m):
+    rng = np.random.default_rng(100 + m)
+    A = rng.uniform(-1, 1, (m, m))
+    B = rng.uniform(-1, 1, (m, m))
+    C, cnt = _leaf(caps, cuda, A, B, scheme="residues")
+    ref, (ta, tb) = _residue_ref(oracle_mod, A, B)
+    assert 53 <= ta <= 55 and 53 <= tb <= 55  # numpy's uniform doubles carry 53 bits
+    assert cnt["split_moduli"] == expected_moduli(ta, tb, m)
+    assert np.array_equal(C, ref)
+
+
+def test_residue_leaf_wide_range_zero_rows_subnormal_results(caps, oracle_mod, cuda):
+    m = 300
+    rng = np.random.default_rng(17)
+    A = rng.uniform(-1, 1, (m, m)) * 2.0 ** rng.integers(-20, 21, (m, m))
+    A[3, :] = 0.0
+    A[:, 5] = 0.0
+    A[7, 11] = 1e-300
+    B = rng.uniform(-1, 1, (m, m)) * 1e-200
+    B[:, 2] = 0.0
+    B[4, 9] = -3e-310  # subnormal operand
+    C, cnt = _leaf(caps, cuda, A, B, scheme="residues")
+    ref, t = _residue_ref(oracle_mod, A, B)
+    assert cnt["split_moduli"] == expected_moduli(t[0], t[1], m)
+    assert np.array_equal(C, ref)
+    assert np.all(C[3, :] == 0) and np.all(C[:, 2] == 0)
+    # products below the normal range: rounded once at 2^-1074
+    A = rng.uniform(-1, 1, (m, m)) * 1e-160
+    B = rng.uniform(-1, 1, (m, m)) * 1e-160
+    C, cnt = _leaf(caps, cuda, A, B, scheme="residues")
+    ref, t = _residue_ref(oracle_mod, A, B)
+    assert np.array_equal(C, ref)
+    assert np.any((C != 0) & (np.abs(C) < 2.2250738585072014e-308))
+
+
+@pytest.mark.parametrize("m,lim", [(256, 1024), (640, 9), (2048, 1024), (96, 2 ** 26)])
+def test_residue_leaf_integers_exact(caps, oracle_mod, cuda, m, lim):
+    rng = np.random.default_rng(m + lim)
+    A = rng.integers(-lim, lim + 1, (m, m)).astype(np.float64)
+    B = rng.integers(-lim, lim + 1, (m, m)).astype(np.float64)
+    C, cnt = _leaf(caps, cuda, A, B, scheme="residues")
+    bits = max(int(np.max(np.abs(A))).bit_length(), int(np.max(np.abs(B))).bit_length()) + 1
+    assert 0 < cnt["split_moduli"] <= expected_moduli(bits, bits, m)
+    if m <= 640:
+        ref, t = _residue_ref(oracle_mod, A, B)
+        assert cnt["split_moduli"] == expected_moduli(t[0], t[1], m)
+        assert np.array_equal(C, ref)
+    if m * lim * lim < 2 ** 53:
+        exact = (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64)
+    else:  # Python integers, each rounded once to double
+        ex = A.astype(np.int64).astype(object) @ B.astype(np.int64).astype(object)
+        exact = np.array([[float(v) for v in row] for row in ex])
+    assert np.array_equal(C, exact)
+
+
+def test_auto_scheme_choice(caps, oracle_mod, cuda):
+    """Float data: residues (16-17 products instead of 36 digit pairs);
+    small integers: digits (1 to 3 digit pairs)."""
+    m = 512
+    rng = np.random.default_rng(3)
+    A = rng.uniform(-1, 1, (m, m))
+    B = rng.uniform(-1, 1, (m, m))
+    C, cnt = _leaf(caps, cuda, A, B)
+    assert cnt["split_moduli"] >= 16 and cnt["split_slices"] == 0
+    assert np.array_equal(C, _residue_ref(oracle_mod, A, B)[0])
+    Ai = rng.integers(-1024, 1025, (m, m)).astype(np.float64)
+    Bi = rng.integers(-1024, 1025, (m, m)).astype(np.float64)
+    C, cnt = _leaf(caps, cuda, Ai, Bi)
+    assert cnt["split_moduli"] == 0 and cnt["split_slices"] == 2
+
+
+def test_residue_scheme_falls_back_to_digits_above_2048(caps, oracle_mod, cuda):
+    m = 2064
+    rng = np.random.default_rng(8)
+    A = rng.uniform(-1, 1, (m, m))
+    B = rng.uniform(-1, 1, (m, m))
+    Cr, cnt_r = _leaf(caps, cuda, A, B, scheme="residues")
+    Cd, cnt_d = _leaf(caps, cuda, A, B, scheme="digits")
+    assert cnt_r["split_moduli"] == 0 and cnt_r["split_slices"] == 8
+    assert np.array_equal(Cr, Cd)

@@ -157,3 +157,76 @@ def test_split_model_float_error(oracle_mod):
     C = C.reshape(m, m).T
     ab = np.abs(A) @ np.abs(B)
     assert np.max(np.abs((C - hi) - lo) / ab) < 2.0 ** -48
+
+
+def _residue_model_py(A, B):
+    """Independent statement of the residue scheme's leaf value: scaled
+    integers from exact rational arithmetic, product in Python integers,
+    one correctly rounded division by a power of two."""
+    import math
+    from fractions import Fraction
+    m = A.shape[0]
+
+    def low_bit(v):  # exponent of the lowest set bit of v != 0
+        fr = Fraction(abs(v))
+        if fr.denominator > 1:
+            return -(fr.denominator.bit_length() - 1)  # odd numerator over 2^k
+        n = fr.numerator
+        return (n & -n).bit_length() - 1
+
+    def line_scales(lines):
+        E, bits = [], 0
+        for line in lines:
+            nz = [v for v in line if v != 0.0]
+            if not nz:
+                E.append(None)
+                continue
+            e = max(math.frexp(v)[1] for v in nz)  # |v| < 2^e
+            lsb = min(low_bit(v) for v in nz)
+            E.append(e)
+            bits = max(bits, e - lsb + 1)
+        return E, min(bits, 55)
+
+    def rnd(x):  # round half to even of a Fraction
+        f = math.floor(x)
+        d = x - f
+        return f + (1 if d > Fraction(1, 2) or (d == Fraction(1, 2) and f % 2) else 0)
+
+    Ea, ta = line_scales([A[i, :] for i in range(m)])
+    Eb, tb = line_scales([B[:, j] for j in range(m)])
+    X = [[0 if Ea[i] is None else rnd(Fraction(A[i, k]) * Fraction(2) ** (ta - Ea[i])) for k in range(m)]
+         for i in range(m)]
+    Y = [[0 if Eb[j] is None else rnd(Fraction(B[k, j]) * Fraction(2) ** (tb - Eb[j])) for k in range(m)]
+         for j in range(m)]
+    C = np.zeros((m, m))
+    for i in range(m):
+        for j in range(m):
+            if Ea[i] is None or Eb[j] is None:
+                continue
+            s = sum(X[i][k] * Y[j][k] for k in range(m))
+            sh = (ta - Ea[i]) + (tb - Eb[j])
+            C[i, j] = s / 2 ** sh if sh >= 0 else float(s * 2 ** -sh)  # int / int: correctly rounded
+    return C, (ta, tb)
+
+
+@pytest.mark.parametrize("kind", ["uniform", "wide", "ints", "tiny"])
+def test_residue_model_matches_exact_rounding(oracle_mod, kind):
+    m = 12
+    rng = np.random.default_rng(len(kind))
+    if kind == "uniform":
+        A, B = rng.uniform(-1, 1, (m, m)), rng.uniform(-1, 1, (m, m))
+    elif kind == "wide":
+        A = rng.uniform(-1, 1, (m, m)) * 2.0 ** rng.integers(-20, 21, (m, m))
+        B = rng.uniform(-1, 1, (m, m)) * 2.0 ** rng.integers(-20, 21, (m, m))
+    elif kind == "ints":
+        A = rng.integers(-2 ** 30, 2 ** 30, (m, m)).astype(np.float64)
+        B = rng.integers(-2 ** 30, 2 ** 30, (m, m)).astype(np.float64)
+    else:
+        A = rng.uniform(-1, 1, (m, m)) * 1e-160
+        B = rng.uniform(-1, 1, (m, m)) * 1e-160
+        A[2, :] = 0.0
+        B[5, 7] = 5e-324
+    C, t = oracle_mod.split_gemm_residues(A.T.copy().reshape(-1), B.T.copy().reshape(-1), m)
+    Cp, tp = _residue_model_py(A, B)
+    assert t == tp
+    assert np.array_equal(C.reshape(m, m).T, Cp)

@@ -29,7 +29,7 @@ def test_noalloc_matches_allocating_entry_point_twice(caps, cuda):
         for m in (512, 200):
             A, B = _inputs(m, 100 * call + m, cuda)
             ref = torch.full_like(A, float("nan"))
-            caps.leaf_gemm(A, B, ref, m, form="split")
+            caps.leaf_gemm(A, B, ref, m, form="split", scheme="digits")  # the scheme the no-allocation path runs
             got = torch.full_like(A, float("nan"))
             st = L.caps_leaf_gemm_split_noalloc_dev(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(B.data_ptr()),
                                                     ctypes.c_void_p(got.data_ptr()), m, 0, 0, stream)
