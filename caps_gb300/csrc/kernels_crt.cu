@@ -480,6 +480,34 @@ __device__ __forceinline__ unsigned long long round_scaled_bits(uint64_t hi, uin
     return sign | (((unsigned long long)(ex + 1074) << 52) + mant);
 }
 
+// The same for the common case, without divergent branches: |v| is shifted
+// so that its top bit is bit 127 (top: bits 127..64, rest: 63..0); a normal
+// result's significand is then top >> 11, its round bit top bit 10 and its
+// sticky bits the rest.  Results below the normal range take the general path.
+__device__ __forceinline__ unsigned long long round_scaled_bits_fast(uint64_t hi, uint64_t lo, bool neg, int e) {
+    if ((hi | lo) == 0) return 0;
+    const int lz = hi ? __clzll((long long)hi) : 64 + __clzll((long long)lo);
+    const int ex = 128 - lz - 53 + e;  // last place of a normal result
+    if (ex < -1074) return round_scaled_bits(hi, lo, neg, e);
+    uint64_t top, rest;
+    if (lz >= 64) {
+        top = lo << (lz - 64);
+        rest = 0;
+    } else if (lz == 0) {
+        top = hi;
+        rest = lo;
+    } else {
+        top = (hi << lz) | (lo >> (64 - lz));
+        rest = lo << lz;
+    }
+    uint64_t mant = top >> 11;
+    const uint64_t rb = (top >> 10) & 1, st = (top & 0x3FFull) | rest;
+    mant += rb & ((st != 0) | (mant & 1));
+    const unsigned long long sign = neg ? 0x8000000000000000ull : 0ull;
+    if (ex > 971) return sign | 0x7FF0000000000000ull;  // |result| >= 2^1024
+    return sign | (((unsigned long long)(ex + 1074) << 52) + mant);
+}
+
 }  // namespace
 
 // One thread = 4 consecutive rows of one column of one leaf; a warp = the
@@ -528,9 +556,10 @@ __global__ void __launch_bounds__(256) crt_combine_kernel(const LeafTask *__rest
             }
         }
     }
-    const uint64_t Mlo = (uint64_t)c_crt.M[L - 1][0] | ((uint64_t)c_crt.M[L - 1][1] << 32);
-    const uint64_t Mhi = (uint64_t)c_crt.M[L - 1][2] | ((uint64_t)c_crt.M[L - 1][3] << 32);
-    const u128 Mv = ((u128)Mhi << 64) | Mlo;
+    uint32_t Mw[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) Mw[k] = c_crt.M[L - 1][k];
+    const u128 Mv = ((u128)(((uint64_t)Mw[3] << 32) | Mw[2]) << 64) | (((uint64_t)Mw[1] << 32) | Mw[0]);
     const u128 Mhalf = Mv >> 1;
     const float minv = c_crt.m_inv[L - 1];
 
@@ -540,32 +569,44 @@ __global__ void __launch_bounds__(256) crt_combine_kernel(const LeafTask *__rest
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         const int64_t i = i0 + q;
-        // carry the column sums into a 128-bit S < L M_L < 2^128
+        // carry the column sums into S = w3..w0 < L M_L < 2^128
+        uint32_t w[4];
         uint64_t c = s[q][0];
-        const uint32_t w0 = (uint32_t)c;
+        w[0] = (uint32_t)c;
         c = s[q][1] + (c >> 32);
-        const uint32_t w1 = (uint32_t)c;
+        w[1] = (uint32_t)c;
         c = s[q][2] + (c >> 32);
-        const uint32_t w2 = (uint32_t)c;
+        w[2] = (uint32_t)c;
         c = s[q][3] + (c >> 32);
-        const uint64_t Slo = ((uint64_t)w1 << 32) | w0, Shi = (c << 32) | w2;
-        const u128 S = ((u128)Shi << 64) | Slo;
-        // S mod M_L: the fp32 quotient is within 1 of floor(S / M_L) (<= 16)
-        const float sf = fmaf((float)Shi, 18446744073709551616.0f, (float)Slo);
-        int qe = (int)(sf * minv);
-        qe = qe < 0 ? 0 : qe;
-        u128 qm = (u128)(uint32_t)qe * Mv;
-        if (qm > S) qm -= Mv;
-        u128 Cr = S - qm;
-        if (Cr >= Mv) Cr -= Mv;
-        // centre: C' in (-M/2, M/2)
-        const bool neg = Cr > Mhalf;
-        const u128 mag = neg ? Mv - Cr : Cr;
+        w[3] = (uint32_t)c;
+        // qe = S / M_L rounded (<= 17) from an fp32 estimate of S (32-bit
+        // conversions: 64-bit ones run on the FP64 pipe); then
+        // C' = S - qe M_L in 32-bit limbs with a signed carry
+        const float sf = fmaf((float)w[3], 7.9228162514264337593543950336e28f,
+                              fmaf((float)w[2], 18446744073709551616.0f, fmaf((float)w[1], 4294967296.0f, (float)w[0])));
+        const long long qe = (long long)__float2int_rn(sf * minv);
+        long long t = 0;
+        uint32_t r[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            t += (long long)w[k] - qe * (long long)Mw[k];
+            r[k] = (uint32_t)t;
+            t >>= 32;
+        }
+        const u128 Cr = ((u128)(((uint64_t)r[3] << 32) | r[2]) << 64) | (((uint64_t)r[1] << 32) | r[0]);
+        // two's complement: centre into (-M/2, M/2] (qe may be one off when
+        // S / M_L lies near a half-integer)
+        bool neg = (r[3] >> 31) != 0;
+        u128 mag = neg ? (u128)0 - Cr : Cr;
+        if (mag > Mhalf) {
+            mag = Mv - mag;  // C' -+ M_L has the other sign
+            neg = !neg;
+        }
         const int ei = i < M ? reinterpret_cast<const int *>(sc + g.off_ea)[i] : 0;
         // C = C' 2^(E_i + E_j - ta - tb); a zero row / column has C' = 0
         if (ei != 0 && ej != 0)
-            outb[q] = round_scaled_bits((uint64_t)(mag >> 64), (uint64_t)mag, neg,
-                                        (ei - 4096) + (ej - 4096) - h->ta - h->tb);
+            outb[q] = round_scaled_bits_fast((uint64_t)(mag >> 64), (uint64_t)mag, neg,
+                                             (ei - 4096) + (ej - 4096) - h->ta - h->tb);
     }
     if (i0 + 3 < M && ((uintptr_t)(C + i0 + j * M) & 15) == 0) {
         double2 *dst = reinterpret_cast<double2 *>(C + i0 + j * M);
