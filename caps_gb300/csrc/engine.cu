@@ -217,6 +217,10 @@ static void emit_leaf_gemm(Builder &b, const std::vector<Prob> &P, int64_t m) {
         int g = (int)std::max<size_t>(1, std::min<size_t>(P.size(), cap / std::max<size_t>(per, 1)));
         g = std::min(g, 65535);
         if (b.split_group > 0) g = std::min(g, b.split_group);
+        // balanced groups: 49 leaves at most 24 to a group run as 17 + 16 + 16,
+        // not 24 + 24 + 1 (a short last group leaves most SMs idle)
+        const size_t ngroups = (P.size() + g - 1) / g;
+        g = (int)((P.size() + ngroups - 1) / ngroups);
         for (size_t s = 0; s < P.size(); s += g) {
             size_t e = std::min(P.size(), s + g);
             std::vector<LeafTask> t;
