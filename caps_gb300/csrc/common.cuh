@@ -99,7 +99,7 @@ cudaError_t launch_dmma_gemm(const LeafTask *tasks_dev, int count, int m, cudaSt
 // the exponent scan (no host round trip):
 //   digits   -- balanced base-128 digit slices, digit-pair products
 //               (kernels_split.cu);
-//   residues -- residues modulo up to 16 small coprime moduli, one product per
+//   residues -- residues modulo up to 17 small coprime moduli, one product per
 //               modulus, exact CRT reconstruction (kernels_crt.cu).
 // Workspace per leaf: see split_workspace_bytes().
 struct SplitParams {

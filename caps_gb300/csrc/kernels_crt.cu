@@ -7,7 +7,7 @@
 //
 //  1. scale (shared with the digit scheme): per row i of A the exponent
 //     bound E_i and lowest set bit, per column j of B the same; t_a, t_b =
-//     min(bits needed over the launch group, 52);
+//     min(bits needed over the launch group, 55);
 //     A'_ik = round(a_ik 2^(t_a - E_i)), B'_kj = round(b_kj 2^(t_b - E_j)),
 //     |A'| <= 2^t_a, |B'| <= 2^t_b, exact when the data needs <= t bits.
 //  2. resolve: the fewest moduli L whose product M_L exceeds
@@ -26,11 +26,8 @@
 //     C = C' 2^(E_i + E_j - t_a - t_b) with one rounding to FP64.
 //
 // Against the digit scheme's 36 digit-pair products for float data, this
-// takes 16 modular products: 52 + 52 bits of operands and 11 of K need
-// 2^116 < M_16.  52 bits per operand (relative to its row's or column's
-// largest entry) keep the leaf product's error well below the FP64
-// rounding of the Strassen sums around it, and the product of the truncated
-// operands is exact (no dropped digit pairs).
+// takes 17 modular products for the same 55-bit operand truncation, and its
+// product of the truncated operands is exact (no dropped digit pairs).
 #include "split_common.cuh"
 
 namespace caps {
@@ -41,7 +38,7 @@ namespace {
 
 // moduli, largest first; any prefix is pairwise coprime
 constexpr int MODULI[LMAX] = {181, 180, 179, 173, 169, 167, 163, 161, 157,
-                              151, 149, 139, 137, 131, 127, 121};
+                              151, 149, 139, 137, 131, 127, 121, 113};
 
 constexpr int RSTAGE_K = 4;                       // 16-deep K steps per stage (K = 64)
 constexpr int RNSTAGE = 4;
@@ -128,7 +125,7 @@ __device__ __forceinline__ float small_int_to_float(int a) {  // |a| < 2^22
 }
 
 // Residues of X = round(x 2^f) modulo the first L moduli, balanced
-// (|r| <= 90).  X (|X| <= 2^52) is cut into four balanced 14-bit limbs a_k
+// (|r| <= 90).  X (|X| <= 2^55) is cut into four balanced 14-bit limbs a_k
 // (X + 8192 (1 + 2^14 + 2^28 + 2^42) has ordinary base-16384 digits
 // a_k + 8192; |a_k| <= 8192); then y = sum_k a_k (2^(14k) mod p), balanced,
 // has |y| < 2^21.1 and is exact in fp32, and r = y - p q with q = y * fl(1/p)
@@ -176,7 +173,7 @@ __global__ void crt_resolve_kernel(char *__restrict__ ws, Geo g, SplitParams p) 
     resolve_sd(h, p, s, nd);
     h->s_used = s;
     h->nd_used = nd;
-    const int ta = h->bitsA < RTMAX ? h->bitsA : RTMAX, tb = h->bitsB < RTMAX ? h->bitsB : RTMAX;
+    const int ta = h->bitsA < 55 ? h->bitsA : 55, tb = h->bitsB < 55 ? h->bitsB : 55;
     int residues = 0, L = 0;
     const bool forced_digits = p.scheme == SCHEME_DIGITS || (p.scheme == SCHEME_AUTO && p.slices > 0);
     if (g.residues_ok && !forced_digits) {
@@ -582,7 +579,7 @@ __global__ void __launch_bounds__(256) crt_combine_kernel(const LeafTask *__rest
         w[2] = (uint32_t)c;
         c = s[q][3] + (c >> 32);
         w[3] = (uint32_t)c;
-        // qe = S / M_L rounded (<= L) from an fp32 estimate of S (32-bit
+        // qe = S / M_L rounded (<= 17) from an fp32 estimate of S (32-bit
         // conversions: 64-bit ones run on the FP64 pipe); then
         // C' = S - qe M_L in 32-bit limbs with a signed carry
         const float sf = fmaf((float)w[3], 7.9228162514264337593543950336e28f,

@@ -13,8 +13,7 @@ constexpr int TN = 64;         // digit scheme: columns of B per diagonal region
 constexpr int TK = 16;         // K per MMA
 constexpr int MAXS = 8;        // digit scheme: max digits
 constexpr int RTN = 256;       // residue scheme: columns of B per tile (one MMA)
-constexpr int LMAX = 16;       // residue scheme: max moduli
-constexpr int RTMAX = 52;      // residue scheme: max bits per scaled operand
+constexpr int LMAX = 17;       // residue scheme: max moduli
 constexpr int RKMAX = 2048;    // residue scheme: max K (K * 90^2 < 2^24: exact fp32 sums)
 constexpr uint32_t WAIT_LIMIT = 1u << 25;
 
@@ -30,7 +29,7 @@ struct SplitHdr {
     int bitsA;     // max over rows of A of E - lsb + 1 (finalize)
     int bitsB;     // the same over the columns of B
     int residues;  // 1: the residue scheme runs (resolve)
-    int ta, tb;    // residue scheme: |A'| <= 2^ta, |B'| <= 2^tb (ta, tb <= RTMAX)
+    int ta, tb;    // residue scheme: |A'| <= 2^ta, |B'| <= 2^tb
     int pad[55];
 };
 static_assert(sizeof(SplitHdr) == 256, "split header is 256 bytes");

@@ -474,7 +474,7 @@ void caps_oracle_split_gemm(int64_t m, const double *A, const double *B, int s, 
 /* integers, independent of the moduli, and rounds it the same way.        */
 /*                                                                         */
 /* Per row i of A: E_i = max exponent bound, lsb_i = min lowest set bit;   */
-/* t_a = min(max_i (E_i - lsb_i + 1), 52), fa_i = t_a - E_i, and           */
+/* t_a = min(max_i (E_i - lsb_i + 1), 55), fa_i = t_a - E_i, and           */
 /* X_ik = round-half-even(a_ik 2^fa_i); the same per column of B.          */
 /* C_ij = sum_k X_ik Y_kj (exact) times 2^-(fa_i + fb_j), rounded once to   */
 /* the nearest double (ties to even, subnormals included).                 */
@@ -545,8 +545,8 @@ void caps_oracle_split_gemm_residues(int64_t m, const double *A, const double *B
     int *Ea = (int *)malloc((size_t)m * sizeof(int));
     int *Eb = (int *)malloc((size_t)m * sizeof(int));
     int ta = residue_scales(m, A, 0, Ea), tb = residue_scales(m, B, 1, Eb);
-    if (ta > 52) ta = 52;  /* the GPU residue scheme's operand width */
-    if (tb > 52) tb = 52;
+    if (ta > 55) ta = 55;
+    if (tb > 55) tb = 55;
     if (t_out) { t_out[0] = ta; t_out[1] = tb; }
     int64_t *X = (int64_t *)malloc((size_t)(m * m) * sizeof(int64_t));  /* row-major X[i][k] */
     int64_t *Y = (int64_t *)malloc((size_t)(m * m) * sizeof(int64_t));  /* Y[j][k] */

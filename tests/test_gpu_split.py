@@ -119,7 +119,7 @@ def test_split_error_no_worse_than_plain(caps, oracle_mod, cuda, wide, scheme):
 
 
 # ---------------------------------------------------------------- residue scheme
-MODULI = [181, 180, 179, 173, 169, 167, 163, 161, 157, 151, 149, 139, 137, 131, 127, 121]
+MODULI = [181, 180, 179, 173, 169, 167, 163, 161, 157, 151, 149, 139, 137, 131, 127, 121, 113]
 
 
 def expected_moduli(ta, tb, m):
@@ -147,7 +147,7 @@ def test_residue_leaf_bitexact_vs_model_uniform(caps, oracle_mod, cuda, m):
     B = rng.uniform(-1, 1, (m, m))
     C, cnt = _leaf(caps, cuda, A, B, scheme="residues")
     ref, (ta, tb) = _residue_ref(oracle_mod, A, B)
-    assert (ta, tb) == (52, 52)  # the residue scheme's cap (numpy's uniform doubles carry 53 bits)
+    assert 53 <= ta <= 55 and 53 <= tb <= 55  # numpy's uniform doubles carry 53 bits
     assert cnt["split_moduli"] == expected_moduli(ta, tb, m)
     assert np.array_equal(C, ref)
 
@@ -197,14 +197,14 @@ def test_residue_leaf_integers_exact(caps, oracle_mod, cuda, m, lim):
 
 
 def test_auto_scheme_choice(caps, oracle_mod, cuda):
-    """Float data: residues (16 products instead of 36 digit pairs);
+    """Float data: residues (16-17 products instead of 36 digit pairs);
     small integers: digits (1 to 3 digit pairs)."""
     m = 512
     rng = np.random.default_rng(3)
     A = rng.uniform(-1, 1, (m, m))
     B = rng.uniform(-1, 1, (m, m))
     C, cnt = _leaf(caps, cuda, A, B)
-    assert cnt["split_moduli"] == 16 and cnt["split_slices"] == 0
+    assert cnt["split_moduli"] >= 16 and cnt["split_slices"] == 0
     assert np.array_equal(C, _residue_ref(oracle_mod, A, B)[0])
     Ai = rng.integers(-1024, 1025, (m, m)).astype(np.float64)
     Bi = rng.integers(-1024, 1025, (m, m)).astype(np.float64)

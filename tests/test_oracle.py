@@ -185,7 +185,7 @@ def _residue_model_py(A, B):
             lsb = min(low_bit(v) for v in nz)
             E.append(e)
             bits = max(bits, e - lsb + 1)
-        return E, min(bits, 52)
+        return E, min(bits, 55)
 
     def rnd(x):  # round half to even of a Fraction
         f = math.floor(x)
