@@ -120,13 +120,10 @@ cudaError_t launch_split_prep(const LeafTask *tasks_dev, int count, int m, Split
 // call before a stream capture.
 void split_gemm_prepare();
 // The tensor-core slice products: the digit-pair GEMM with its exact
-// recombination epilogue, or the per-modulus residue GEMM.
+// recombination epilogue, or the per-modulus residue GEMM with its CRT
+// reconstruction warps.
 cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, SplitParams p,
                               void *workspace, unsigned int *status_dev, cudaStream_t stream);
-// Residue scheme only: CRT reconstruction of C from the product residues
-// (returns at once when the digit scheme ran).
-cudaError_t launch_split_combine(const LeafTask *tasks_dev, int count, int m, SplitParams p,
-                                 void *workspace, cudaStream_t stream);
 
 // kernels_crt.cu, called by the launchers above
 cudaError_t crt_prepare();

@@ -207,14 +207,20 @@ static void emit_event(Builder &b, int kind, int index) {
     b.ops.push_back(o);
 }
 
+// Split-form scratch of one launch group: the slice planes of its leaves
+// (285 MB per residue-scheme leaf of 2048) and fixed parts.  Larger groups
+// give the persistent GEMMs more work units to balance over the SMs.
+static const size_t kSplitGroupBytes = (size_t)16 << 30;
+
 static void emit_leaf_gemm(Builder &b, const std::vector<Prob> &P, int64_t m) {
     if (b.opt.form == CAPS_FORM_SPLIT) {
         // bound split scratch: groups of leaves (the grid's z extent bounds
-        // the count too)
+        // the count too); per leaf = the marginal bytes, over the fixed part
         const int scheme = b.opt.split_scheme;
-        size_t per = split_workspace_bytes((int)m, 1, scheme);
-        size_t cap = (size_t)8 << 30;  // 8 GiB of slice planes per launch group
-        int g = (int)std::max<size_t>(1, std::min<size_t>(P.size(), cap / std::max<size_t>(per, 1)));
+        const size_t one = split_workspace_bytes((int)m, 1, scheme);
+        const size_t per = split_workspace_bytes((int)m, 2, scheme) - one, fixed = one - per;
+        const size_t room = kSplitGroupBytes > fixed ? kSplitGroupBytes - fixed : per;
+        int g = (int)std::max<size_t>(1, std::min<size_t>(P.size(), room / std::max<size_t>(per, 1)));
         g = std::min(g, 65535);
         if (b.split_group > 0) g = std::min(g, b.split_group);
         // balanced groups: 49 leaves at most 24 to a group run as 17 + 16 + 16,
@@ -482,7 +488,7 @@ static void auto_pattern(const caps_desc &d, const caps_options &o, char *out) {
             n /= 2;
         }
         if (o.form == CAPS_FORM_SPLIT)
-            total += (int64_t)std::min<size_t>(split_workspace_bytes((int)n, (int)count, o.split_scheme), (size_t)8 << 30);
+            total += (int64_t)std::min<size_t>(split_workspace_bytes((int)n, (int)count, o.split_scheme), kSplitGroupBytes);
         if (total > budget) {
             out[l] = 'd';
             break;
@@ -583,27 +589,7 @@ static caps_status launch_ops(const std::vector<Op> &ops, char *tables, char *ws
                 r.phase = PH_MUL;
                 r.gemm = true;
                 r.m3 = (double)o.count * o.m * (double)o.m * o.m;
-                if (err != cudaSuccess) break;
-                if (timed) {
-                    cudaEventCreate(&r.e1);
-                    cudaEventRecord(r.e1, s);
-                    recs.push_back(r);
-                }
-                // residue scheme: the CRT reconstruction, timed with the
-                // multiply phase but not as GEMM (returns at once for digits)
-                Rec post{nullptr, nullptr, PH_MUL, false, 0.0};
-                if (timed) ev_begin(post.e0);
-                err = launch_split_combine(t, o.count, o.m, o.sp, ws, s);
-                if (err != cudaSuccess) {
-                    note_cuda_error(err, "kernel launch");
-                    return CAPS_ERR_CUDA;
-                }
-                if (timed) {
-                    cudaEventCreate(&post.e1);
-                    cudaEventRecord(post.e1, s);
-                    recs.push_back(post);
-                }
-                continue;
+                break;
             }
             case K_WAIT:
                 err = cudaStreamWaitEvent(s, g_host_events[o.count], 0);

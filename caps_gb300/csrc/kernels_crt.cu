@@ -18,11 +18,12 @@
 //     written as pre-tiled UMMA canonical K-major planes like the digits.
 //  4. gemm:    per modulus, sum_k rA rB on tcgen05.mma kind::f16
 //     (bf16 x bf16 -> f32): |sum| <= K 90^2 < 2^24 for K <= 2048, so the
-//     fp32 accumulator is exact.  The epilogue reduces it modulo p_l and
-//     stores z_l = (c mod p_l) y_l mod p_l, y_l = (M_L / p_l)^-1 mod p_l,
-//     one byte per element.
-//  5. combine: S = sum_l z_l (M_L / p_l) < L M_L is reduced modulo M_L and
-//     centred into (-M_L/2, M_L/2): that is C' exactly; then
+//     fp32 accumulator is exact.  Drain warps reduce it modulo p_l and keep
+//     z_l = (c mod p_l) y_l mod p_l, y_l = (M_L / p_l)^-1 mod p_l, one byte
+//     per element, in a product-residue tile of the CTA.
+//  5. CRT (reconstruction warps of the same kernel, overlapping the next
+//     tile's MMAs): S = sum_l z_l (M_L / p_l) < L M_L is reduced modulo M_L
+//     and centred into (-M_L/2, M_L/2): that is C' exactly; then
 //     C = C' 2^(E_i + E_j - t_a - t_b) with one rounding to FP64.
 //
 // Against the digit scheme's 36 digit-pair products for float data, this
@@ -47,7 +48,7 @@ constexpr int RB_TILE = RTN * TK * 2;             // 8 KiB: 256 x 16 bf16
 constexpr int RSTAGE_A = RSTAGE_K * RA_TILE;      // 16 KiB
 constexpr int RSTAGE_B = RSTAGE_K * RB_TILE;      // 32 KiB
 constexpr int RSTAGE_BYTES = RSTAGE_A + RSTAGE_B; // 48 KiB
-constexpr int RGEMM_THREADS = 320;                // producer, MMA, 8 epilogue warps
+constexpr int RGEMM_THREADS = 448;                // producer, MMA, 8 drain, 4 reconstruction warps
 constexpr unsigned RSTATUS = 0x100;               // status bits of this kernel: RSTATUS << code
 
 struct CrtTables {
@@ -261,182 +262,7 @@ __global__ void __launch_bounds__(256) crt_slice_kernel(const LeafTask *__restri
     }
 }
 
-// ---------------------------------------------------------------- gemm
-// Persistent, one CTA per SM, 320 threads: warp 0 loads (one lane, bulk
-// copies of pre-tiled planes), warp 1 issues the MMAs (one lane), warps 2..9
-// drain the accumulators.  A work unit is (leaf, modulus, 128-row tile,
-// 256-column tile): Kp / 16 MMAs of 128 x 256 x 16 into one of two TMEM
-// accumulators of 256 columns, so the epilogue drains one unit while the
-// next accumulates.  Units are ordered leaf, modulus, row tile, column tile:
-// the CTAs running at one time share the A and B planes of one modulus of
-// one leaf (16 MB at m = 2048) through L2.
-__global__ void __launch_bounds__(RGEMM_THREADS, 1)
-    crt_gemm_kernel(char *__restrict__ ws, Geo g, unsigned *__restrict__ status) {
-    const SplitHdr *h = reinterpret_cast<const SplitHdr *>(ws);
-    if (!h->residues) return;  // the digit scheme runs
-    const int L = h->moduli;
-    extern __shared__ __align__(1024) unsigned char smem_raw[];
-    unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    unsigned char *stA = smem;                        // RNSTAGE x RSTAGE_A
-    unsigned char *stB = smem + RNSTAGE * RSTAGE_A;   // RNSTAGE x RSTAGE_B
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + RNSTAGE * RSTAGE_BYTES);
-    // bars: full[RNSTAGE], empty[RNSTAGE], tfull[2], tempty[2], final
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * RNSTAGE + 5);
-    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + RNSTAGE);
-    const uint32_t tfull0 = smem_u32(bars + 2 * RNSTAGE), tempty0 = smem_u32(bars + 2 * RNSTAGE + 2);
-    const uint32_t finalb = smem_u32(bars + 2 * RNSTAGE + 4);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-
-    if (threadIdx.x == 0) {
-        for (int i = 0; i < RNSTAGE; i++) {
-            mbar_init(full0 + 8 * i, 1);
-            mbar_init(empty0 + 8 * i, 1);
-        }
-        for (int i = 0; i < 2; i++) {
-            mbar_init(tfull0 + 8 * i, 1);
-            mbar_init(tempty0 + 8 * i, 8);
-        }
-        mbar_init(finalb, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    if (warp == 1) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
-                         smem_u32(tmem_slot))
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem = *tmem_slot;
-
-    const int64_t tiles = (int64_t)g.mtiles * g.rtiles;
-    const int64_t per_leaf = tiles * L;
-    const int64_t total = per_leaf * g.count;
-    const int nks = g.nks;
-
-    if (warp == 0) {
-        // ------------------------------------------------ producer
-        if (lane == 0) {
-            int stage = 0;
-            uint32_t phase = 0;
-            bool ok = true;
-            uint32_t armed[RNSTAGE] = {0, 0, 0, 0};  // 1 + phase of the last arm
-            for (int64_t u = blockIdx.x; u < total && ok; u += gridDim.x) {
-                const int leafi = (int)(u / per_leaf);
-                const int64_t rem = u % per_leaf;
-                const int l = (int)(rem / tiles);
-                const int64_t tile = rem % tiles;
-                const int mt = (int)(tile / g.rtiles), rt = (int)(tile % g.rtiles);
-                const char *pl = leaf_digits(ws, g, leafi);
-                const char *srcA = pl + g.off_ra + (((size_t)l * g.mtiles + mt) * nks) * RA_TILE;
-                const char *srcB = pl + g.off_rb + (((size_t)l * g.rtiles + rt) * nks) * RB_TILE;
-                for (int ks = 0; ks < nks; ks += RSTAGE_K) {
-                    const uint32_t n = ks + RSTAGE_K <= nks ? RSTAGE_K : (uint32_t)(nks - ks);
-                    if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, status, RSTATUS << 0)) { ok = false; break; }
-                    mbar_expect_tx(full0 + 8 * stage, n * (RA_TILE + RB_TILE));
-                    bulk_g2s(smem_u32(stA + stage * RSTAGE_A), srcA + (size_t)ks * RA_TILE, n * RA_TILE,
-                             full0 + 8 * stage);
-                    bulk_g2s(smem_u32(stB + stage * RSTAGE_B), srcB + (size_t)ks * RB_TILE, n * RB_TILE,
-                             full0 + 8 * stage);
-                    armed[stage] = 1 + phase;
-                    if (++stage == RNSTAGE) { stage = 0; phase ^= 1; }
-                }
-            }
-            // every armed stage's copies land before the CTA exits
-            for (int i = 0; i < RNSTAGE; i++)
-                if (armed[i]) mbar_wait(full0 + 8 * i, armed[i] - 1, status, RSTATUS << 1);
-        }
-    } else if (warp == 1) {
-        // ------------------------------------------------ MMA issuer
-        if (lane == 0) {
-            // K-direction core-matrix stride (LBO) 128 B, row-group stride (SBO) 256 B
-            const uint64_t a0 = sdesc(smem_u32(stA), 128, 256), b0 = sdesc(smem_u32(stB), 128, 256);
-            const uint32_t idesc = idesc_bf16(TM, RTN);
-            int stage = 0;
-            uint32_t phase = 0, uc = 0;
-            bool ok = true;
-            for (int64_t u = blockIdx.x; u < total && ok; u += gridDim.x, uc++) {
-                const uint32_t acc = uc & 1;
-                if (!mbar_wait(tempty0 + 8 * acc, ((uc >> 1) & 1) ^ 1, status, RSTATUS << 2)) { ok = false; break; }
-                tc_fence_after();
-                const uint32_t dt = tmem + acc * RTN;
-                for (int ks = 0; ks < nks; ks += RSTAGE_K) {
-                    const int n = ks + RSTAGE_K <= nks ? RSTAGE_K : nks - ks;
-                    if (!mbar_wait(full0 + 8 * stage, phase, status, RSTATUS << 3)) { ok = false; break; }
-                    tc_fence_after();
-                    const uint64_t sa = (uint64_t)((uint32_t)stage * RSTAGE_A) >> 4;
-                    const uint64_t sb = (uint64_t)((uint32_t)stage * RSTAGE_B) >> 4;
-#pragma unroll
-                    for (int j = 0; j < RSTAGE_K; j++)
-                        if (j < n)
-                            umma(dt, a0 + sa + (uint64_t)(j * RA_TILE >> 4), b0 + sb + (uint64_t)(j * RB_TILE >> 4),
-                                 idesc, (ks + j) > 0 ? 1u : 0u);
-                    umma_commit(empty0 + 8 * stage);
-                    if (++stage == RNSTAGE) { stage = 0; phase ^= 1; }
-                }
-                if (!ok) break;
-                umma_commit(tfull0 + 8 * acc);
-            }
-            // every issued MMA completes before TMEM is released
-            umma_commit(finalb);
-            mbar_wait(finalb, 0, status, RSTATUS << 4);
-        }
-    } else {
-        // ------------------------------------------------ epilogue (8 warps)
-        const int quarter = warp & 3;          // TMEM lanes 32*quarter.. (rows of the tile)
-        const int colhalf = (warp - 2) >> 2;   // columns 128*colhalf.. of the accumulator
-        uint32_t uc = 0;
-        for (int64_t u = blockIdx.x; u < total; u += gridDim.x, uc++) {
-            const int leafi = (int)(u / per_leaf);
-            const int64_t rem = u % per_leaf;
-            const int l = (int)(rem / tiles);
-            const int64_t tile = rem % tiles;
-            const int mt = (int)(tile / g.rtiles), rt = (int)(tile % g.rtiles);
-            const uint32_t acc = uc & 1;
-            // warp-uniform: tcgen05.ld below is .sync.aligned
-            const bool got = mbar_wait(tfull0 + 8 * acc, (uc >> 1) & 1, status, RSTATUS << 5);
-            if (!__all_sync(0xffffffffu, got)) break;
-            tc_fence_after();
-            const float p = c_crt.p[l], invp = c_crt.invp[l], y = c_crt.y[L - 1][l];
-            unsigned char *out = (unsigned char *)leaf_digits(ws, g, leafi) + g.off_ro +
-                                 ((((size_t)l * g.mtiles + mt) * g.rtiles + rt) * RTN) * TM + quarter * 32 + lane;
-#pragma unroll 1
-            for (int c4 = 0; c4 < 4; c4++) {
-                uint32_t v[32];
-                const int col0 = colhalf * 128 + c4 * 32;
-                tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + acc * RTN + col0, v);
-#pragma unroll
-                for (int e = 0; e < 32; e++) {
-                    // c = sum rA rB (exact, |c| < 2^24).  q = c / p rounded by
-                    // MAGIC is floor or ceil of c / p (|c / p| 2^-24 < 1/2 away),
-                    // so c - q p lies in [-p, p) and one correction gives
-                    // r = c mod p in [0, p).
-                    const float c = __uint_as_float(v[e]);
-                    float r = fmaf(-(fmaf(c, invp, MAGIC) - MAGIC), p, c);
-                    r = r < 0.0f ? r + p : r;
-                    // z = r y mod p, the same way (r y < 2^15, exact)
-                    const float ry = r * y;
-                    float z = fmaf(-(fmaf(ry, invp, MAGIC) - MAGIC), p, ry);
-                    z = z < 0.0f ? z + p : z;
-                    out[(size_t)(col0 + e) * TM] = (unsigned char)__float_as_uint(z + MAGIC);  // low byte: z
-                }
-            }
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(tempty0 + 8 * acc);
-        }
-    }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    if (warp == 1) {
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
-    }
-}
-
-// ---------------------------------------------------------------- combine
+// ---------------------------------------------------------------- CRT reconstruction
 namespace {
 
 // The encoding of the double nearest |v| 2^e (ties to even), with the sign
@@ -510,35 +336,18 @@ __device__ __forceinline__ unsigned long long round_scaled_bits_fast(uint64_t hi
 
 }  // namespace
 
-// One thread = 4 consecutive rows of one column of one leaf; a warp = the
-// 128 rows of a tile column, so each residue plane is read as 128
-// consecutive bytes and C written as 1 KiB.
-__global__ void __launch_bounds__(256) crt_combine_kernel(const LeafTask *__restrict__ tasks,
-                                                          char *__restrict__ ws, Geo g) {
-    const SplitHdr *h = reinterpret_cast<const SplitHdr *>(ws);
-    if (!h->residues) return;
-    const int L = h->moduli;
-    const int leafi = blockIdx.y;
-    const int64_t M = g.m;
-    const int64_t colblocks = (M + 7) / 8;
-    const int mt = (int)(blockIdx.x / colblocks);
-    const int64_t j = (blockIdx.x % colblocks) * 8 + (threadIdx.x >> 5);
-    if (mt >= g.mtiles || j >= M) return;
-    const int r0 = (threadIdx.x & 31) * 4;  // row within the tile
-    const int64_t i0 = (int64_t)mt * TM + r0;
-    if (i0 >= M) return;
-    const int rt = (int)(j / RTN), col = (int)(j % RTN);
-    const char *pl = leaf_digits(ws, g, leafi);
-    const char *sc = leaf_scalars(ws, g, leafi);
-    const size_t plane = (size_t)g.mtiles * g.rtiles * RTN * TM;
-    const uint32_t *res = reinterpret_cast<const uint32_t *>(
-        pl + g.off_ro + (((size_t)mt * g.rtiles + rt) * RTN + col) * TM + r0);
+namespace {
 
-    // all residue loads in flight at once: 4 rows of this column per modulus
-    uint32_t zq[LMAX];
-#pragma unroll
-    for (int l = 0; l < LMAX; l++) zq[l] = l < L ? __ldg(res + l * (plane / 4)) : 0u;
-    // S = sum_l z_l (M_L / p_l), in 32-bit limbs with 64-bit column sums
+// C' for 4 consecutive rows of one column from their product-residue bytes:
+// zq[l] holds z_l of the 4 rows (byte q = row q).  S = sum_l z_l M_L / p_l
+// (< L M_L < 2^128) is formed in 32-bit limbs with 64-bit column sums; then
+// qe = S / M_L rounded from an fp32 estimate of S (32-bit conversions: the
+// 64-bit ones run on the FP64 pipe), C' = S - qe M_L in 32-bit limbs with a
+// signed carry, and C' is centred into (-M_L/2, M_L/2] (qe may be one off
+// when S / M_L lies near a half-integer).  out[q] = the FP64 encoding of
+// C'_q 2^e[q], or 0 where zero[q].
+__device__ __forceinline__ void crt_reconstruct4(const uint32_t (&zq)[LMAX], int L, const int (&e)[4],
+                                                 const bool (&zero)[4], unsigned long long (&out)[4]) {
     uint64_t s[4][4];
 #pragma unroll
     for (int q = 0; q < 4; q++)
@@ -562,14 +371,8 @@ __global__ void __launch_bounds__(256) crt_combine_kernel(const LeafTask *__rest
     const u128 Mv = ((u128)(((uint64_t)Mw[3] << 32) | Mw[2]) << 64) | (((uint64_t)Mw[1] << 32) | Mw[0]);
     const u128 Mhalf = Mv >> 1;
     const float minv = c_crt.m_inv[L - 1];
-
-    const int ej = reinterpret_cast<const int *>(sc + g.off_eb)[j];
-    double *C = tasks[leafi].C;
-    unsigned long long outb[4] = {0, 0, 0, 0};
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-        const int64_t i = i0 + q;
-        // carry the column sums into S = w3..w0 < L M_L < 2^128
         uint32_t w[4];
         uint64_t c = s[q][0];
         w[0] = (uint32_t)c;
@@ -579,9 +382,6 @@ __global__ void __launch_bounds__(256) crt_combine_kernel(const LeafTask *__rest
         w[2] = (uint32_t)c;
         c = s[q][3] + (c >> 32);
         w[3] = (uint32_t)c;
-        // qe = S / M_L rounded (<= 17) from an fp32 estimate of S (32-bit
-        // conversions: 64-bit ones run on the FP64 pipe); then
-        // C' = S - qe M_L in 32-bit limbs with a signed carry
         const float sf = fmaf((float)w[3], 7.9228162514264337593543950336e28f,
                               fmaf((float)w[2], 18446744073709551616.0f, fmaf((float)w[1], 4294967296.0f, (float)w[0])));
         const long long qe = (long long)__float2int_rn(sf * minv);
@@ -594,28 +394,270 @@ __global__ void __launch_bounds__(256) crt_combine_kernel(const LeafTask *__rest
             t >>= 32;
         }
         const u128 Cr = ((u128)(((uint64_t)r[3] << 32) | r[2]) << 64) | (((uint64_t)r[1] << 32) | r[0]);
-        // two's complement: centre into (-M/2, M/2] (qe may be one off when
-        // S / M_L lies near a half-integer)
         bool neg = (r[3] >> 31) != 0;
         u128 mag = neg ? (u128)0 - Cr : Cr;
         if (mag > Mhalf) {
             mag = Mv - mag;  // C' -+ M_L has the other sign
             neg = !neg;
         }
-        const int ei = i < M ? reinterpret_cast<const int *>(sc + g.off_ea)[i] : 0;
-        // C = C' 2^(E_i + E_j - ta - tb); a zero row / column has C' = 0
-        if (ei != 0 && ej != 0)
-            outb[q] = round_scaled_bits_fast((uint64_t)(mag >> 64), (uint64_t)mag, neg,
-                                             (ei - 4096) + (ej - 4096) - h->ta - h->tb);
+        out[q] = zero[q] ? 0ull : round_scaled_bits_fast((uint64_t)(mag >> 64), (uint64_t)mag, neg, e[q]);
     }
-    if (i0 + 3 < M && ((uintptr_t)(C + i0 + j * M) & 15) == 0) {
-        double2 *dst = reinterpret_cast<double2 *>(C + i0 + j * M);
-        dst[0] = make_double2(__longlong_as_double((long long)outb[0]), __longlong_as_double((long long)outb[1]));
-        dst[1] = make_double2(__longlong_as_double((long long)outb[2]), __longlong_as_double((long long)outb[3]));
-    } else {
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- gemm
+// Persistent, one CTA per SM, 448 threads: warp 0 loads (one lane, bulk
+// copies of pre-tiled planes), warp 1 issues the MMAs (one lane), warps 2..9
+// drain the accumulators, warps 10..13 reconstruct C.
+//
+// A work unit is (leaf, 128-row tile, 256-column tile).  For each modulus in
+// turn it takes Kp / 16 MMAs of 128 x 256 x 16 into one of two TMEM
+// accumulators of 256 columns; they alternate, so the drain of one modulus
+// overlaps the MMAs of the next.  The drain reduces each exact sum modulo p
+// and stores z = (c mod p) y mod p as a byte into the CTA's product-residue
+// tile: [modulus][column][row], two tiles per CTA used in turn.  When a
+// unit's last modulus is drained, the four reconstruction warps turn that
+// tile into C (CRT, one rounding) while the drain moves on to the next unit's
+// moduli in the other tile; mbarriers hand the tiles back and forth.
+//
+// Units are ordered leaf, row tile, column tile, and the CTAs go through the
+// moduli in step, so the CTAs running at one time share the A and B planes
+// of one modulus of about one leaf (16 MB at m = 2048) through L2.
+__global__ void __launch_bounds__(RGEMM_THREADS, 1)
+    crt_gemm_kernel(const LeafTask *__restrict__ tasks, char *__restrict__ ws, Geo g,
+                    unsigned *__restrict__ status) {
+    const SplitHdr *h = reinterpret_cast<const SplitHdr *>(ws);
+    if (!h->residues) return;  // the digit scheme runs
+    const int L = h->moduli;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char *stA = smem;                        // RNSTAGE x RSTAGE_A
+    unsigned char *stB = smem + RNSTAGE * RSTAGE_A;   // RNSTAGE x RSTAGE_B
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + RNSTAGE * RSTAGE_BYTES);
+    // bars: full[RNSTAGE], empty[RNSTAGE], tfull[2], tempty[2], final, zfull[2], zempty[2]
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * RNSTAGE + 9);
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + RNSTAGE);
+    const uint32_t tfull0 = smem_u32(bars + 2 * RNSTAGE), tempty0 = smem_u32(bars + 2 * RNSTAGE + 2);
+    const uint32_t finalb = smem_u32(bars + 2 * RNSTAGE + 4);
+    const uint32_t zfull0 = smem_u32(bars + 2 * RNSTAGE + 5), zempty0 = smem_u32(bars + 2 * RNSTAGE + 7);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < RNSTAGE; i++) {
+            mbar_init(full0 + 8 * i, 1);
+            mbar_init(empty0 + 8 * i, 1);
+        }
+        for (int i = 0; i < 2; i++) {
+            mbar_init(tfull0 + 8 * i, 1);
+            mbar_init(tempty0 + 8 * i, 8);   // the 8 drain warps
+            mbar_init(zfull0 + 8 * i, 8);    // the 8 drain warps
+            mbar_init(zempty0 + 8 * i, 4);   // the 4 reconstruction warps
+        }
+        mbar_init(finalb, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
+                         smem_u32(tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    const int64_t tiles = (int64_t)g.mtiles * g.rtiles;
+    const int64_t total = tiles * g.count;
+    const int nks = g.nks;
+    unsigned char *ztiles = (unsigned char *)ws + g.z_base + (size_t)blockIdx.x * 2 * ZTILE_BYTES;
+
+    if (warp == 0) {
+        // ------------------------------------------------ producer
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            bool ok = true;
+            uint32_t armed[RNSTAGE] = {0, 0, 0, 0};  // 1 + phase of the last arm
+            for (int64_t u = blockIdx.x; u < total && ok; u += gridDim.x) {
+                const int leafi = (int)(u / tiles);
+                const int64_t tile = u % tiles;
+                const int mt = (int)(tile / g.rtiles), rt = (int)(tile % g.rtiles);
+                const char *pl = leaf_digits(ws, g, leafi);
+                for (int l = 0; l < L && ok; l++) {
+                    const char *srcA = pl + g.off_ra + (((size_t)l * g.mtiles + mt) * nks) * RA_TILE;
+                    const char *srcB = pl + g.off_rb + (((size_t)l * g.rtiles + rt) * nks) * RB_TILE;
+                    for (int ks = 0; ks < nks; ks += RSTAGE_K) {
+                        const uint32_t n = ks + RSTAGE_K <= nks ? RSTAGE_K : (uint32_t)(nks - ks);
+                        if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, status, RSTATUS << 0)) { ok = false; break; }
+                        mbar_expect_tx(full0 + 8 * stage, n * (RA_TILE + RB_TILE));
+                        bulk_g2s(smem_u32(stA + stage * RSTAGE_A), srcA + (size_t)ks * RA_TILE, n * RA_TILE,
+                                 full0 + 8 * stage);
+                        bulk_g2s(smem_u32(stB + stage * RSTAGE_B), srcB + (size_t)ks * RB_TILE, n * RB_TILE,
+                                 full0 + 8 * stage);
+                        armed[stage] = 1 + phase;
+                        if (++stage == RNSTAGE) { stage = 0; phase ^= 1; }
+                    }
+                }
+            }
+            // every armed stage's copies land before the CTA exits
+            for (int i = 0; i < RNSTAGE; i++)
+                if (armed[i]) mbar_wait(full0 + 8 * i, armed[i] - 1, status, RSTATUS << 1);
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            // K-direction core-matrix stride (LBO) 128 B, row-group stride (SBO) 256 B
+            const uint64_t a0 = sdesc(smem_u32(stA), 128, 256), b0 = sdesc(smem_u32(stB), 128, 256);
+            const uint32_t idesc = idesc_bf16(TM, RTN);
+            int stage = 0;
+            uint32_t phase = 0, uc = 0;
+            bool ok = true;
+            for (int64_t u = blockIdx.x; u < total && ok; u += gridDim.x) {
+                for (int l = 0; l < L && ok; l++, uc++) {
+                    const uint32_t acc = uc & 1;
+                    if (!mbar_wait(tempty0 + 8 * acc, ((uc >> 1) & 1) ^ 1, status, RSTATUS << 2)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t dt = tmem + acc * RTN;
+                    for (int ks = 0; ks < nks; ks += RSTAGE_K) {
+                        const int n = ks + RSTAGE_K <= nks ? RSTAGE_K : nks - ks;
+                        if (!mbar_wait(full0 + 8 * stage, phase, status, RSTATUS << 3)) { ok = false; break; }
+                        tc_fence_after();
+                        const uint64_t sa = (uint64_t)((uint32_t)stage * RSTAGE_A) >> 4;
+                        const uint64_t sb = (uint64_t)((uint32_t)stage * RSTAGE_B) >> 4;
 #pragma unroll
-        for (int q = 0; q < 4; q++)
-            if (i0 + q < M) C[i0 + q + j * M] = __longlong_as_double((long long)outb[q]);
+                        for (int j = 0; j < RSTAGE_K; j++)
+                            if (j < n)
+                                umma(dt, a0 + sa + (uint64_t)(j * RA_TILE >> 4), b0 + sb + (uint64_t)(j * RB_TILE >> 4),
+                                     idesc, (ks + j) > 0 ? 1u : 0u);
+                        umma_commit(empty0 + 8 * stage);
+                        if (++stage == RNSTAGE) { stage = 0; phase ^= 1; }
+                    }
+                    if (!ok) break;
+                    umma_commit(tfull0 + 8 * acc);
+                }
+            }
+            // every issued MMA completes before TMEM is released
+            umma_commit(finalb);
+            mbar_wait(finalb, 0, status, RSTATUS << 4);
+        }
+    } else if (warp < 10) {
+        // ------------------------------------------------ drain (8 warps)
+        const int quarter = warp & 3;          // TMEM lanes 32*quarter.. (rows of the tile)
+        const int colhalf = (warp - 2) >> 2;   // columns 128*colhalf.. of the tile
+        const int row = quarter * 32 + lane;
+        uint32_t uc = 0, tc = 0;
+        bool ok = true;
+        for (int64_t u = blockIdx.x; u < total && ok; u += gridDim.x, tc++) {
+            const uint32_t zb = tc & 1;
+            // the reconstruction warps are done with this residue tile
+            const bool free_ = mbar_wait(zempty0 + 8 * zb, ((tc >> 1) & 1) ^ 1, status, RSTATUS << 6);
+            if (!__all_sync(0xffffffffu, free_)) break;
+            unsigned char *zt = ztiles + (size_t)zb * ZTILE_BYTES + row;
+            for (int l = 0; l < L; l++, uc++) {
+                const uint32_t acc = uc & 1;
+                // warp-uniform: tcgen05.ld below is .sync.aligned
+                const bool got = mbar_wait(tfull0 + 8 * acc, (uc >> 1) & 1, status, RSTATUS << 5);
+                if (!__all_sync(0xffffffffu, got)) { ok = false; break; }
+                tc_fence_after();
+                const float p = c_crt.p[l], invp = c_crt.invp[l], y = c_crt.y[L - 1][l];
+                unsigned char *out = zt + (size_t)l * RTN * TM;
+#pragma unroll 1
+                for (int c4 = 0; c4 < 4; c4++) {
+                    uint32_t v[32];
+                    const int col0 = colhalf * 128 + c4 * 32;
+                    tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + acc * RTN + col0, v);
+#pragma unroll
+                    for (int e = 0; e < 32; e++) {
+                        // c = sum rA rB (exact, |c| < 2^24).  q = c / p rounded
+                        // by MAGIC is floor or ceil of c / p (|c / p| 2^-24 < 1/2
+                        // away), so c - q p lies in [-p, p) and one correction
+                        // gives r = c mod p in [0, p).
+                        const float c = __uint_as_float(v[e]);
+                        float r = fmaf(-(fmaf(c, invp, MAGIC) - MAGIC), p, c);
+                        r = r < 0.0f ? r + p : r;
+                        // z = r y mod p, the same way (r y < 2^15, exact)
+                        const float ry = r * y;
+                        float z = fmaf(-(fmaf(ry, invp, MAGIC) - MAGIC), p, ry);
+                        z = z < 0.0f ? z + p : z;
+                        out[(size_t)(col0 + e) * TM] = (unsigned char)__float_as_uint(z + MAGIC);  // low byte: z
+                    }
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(tempty0 + 8 * acc);
+            }
+            if (!ok) break;
+            // the tile's residues are complete: hand it to the reconstruction warps
+            __threadfence_block();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(zfull0 + 8 * zb);
+        }
+    } else {
+        // ------------------------------------------------ reconstruction (4 warps)
+        // one warp = one column of the tile at a time, each lane 4 of its rows
+        const int w = warp - 10;
+        const int64_t M = g.m;
+        uint32_t tc = 0;
+        for (int64_t u = blockIdx.x; u < total; u += gridDim.x, tc++) {
+            const uint32_t zb = tc & 1;
+            const bool got = mbar_wait(zfull0 + 8 * zb, (tc >> 1) & 1, status, RSTATUS << 7);
+            if (!__all_sync(0xffffffffu, got)) break;
+            const int leafi = (int)(u / tiles);
+            const int64_t tile = u % tiles;
+            const int mt = (int)(tile / g.rtiles), rt = (int)(tile % g.rtiles);
+            const char *sc = leaf_scalars(ws, g, leafi);
+            const int *eap = reinterpret_cast<const int *>(sc + g.off_ea);
+            const int *ebp = reinterpret_cast<const int *>(sc + g.off_eb);
+            double *C = tasks[leafi].C;
+            const int64_t i0 = (int64_t)mt * TM + lane * 4;
+            int ei[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) ei[q] = i0 + q < M ? eap[i0 + q] : 0;
+            const unsigned char *zt = ztiles + (size_t)zb * ZTILE_BYTES + lane * 4;
+#pragma unroll 1
+            for (int col = w; col < RTN; col += 4) {
+                const int64_t j = (int64_t)rt * RTN + col;
+                if (j >= M || i0 >= M) continue;
+                uint32_t zq[LMAX];
+#pragma unroll
+                for (int l = 0; l < LMAX; l++)
+                    zq[l] = l < L ? *reinterpret_cast<const uint32_t *>(zt + ((size_t)l * RTN + col) * TM) : 0u;
+                const int ej = ebp[j];
+                int e[4];
+                bool zero[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    // C = C' 2^(E_i + E_j - ta - tb); a zero row / column has C' = 0
+                    zero[q] = ei[q] == 0 || ej == 0;
+                    e[q] = (ei[q] - 4096) + (ej - 4096) - h->ta - h->tb;
+                }
+                unsigned long long out[4];
+                crt_reconstruct4(zq, L, e, zero, out);
+                double *dst = C + i0 + j * M;
+                if (i0 + 3 < M && ((uintptr_t)dst & 15) == 0) {
+                    reinterpret_cast<double2 *>(dst)[0] =
+                        make_double2(__longlong_as_double((long long)out[0]), __longlong_as_double((long long)out[1]));
+                    reinterpret_cast<double2 *>(dst)[1] =
+                        make_double2(__longlong_as_double((long long)out[2]), __longlong_as_double((long long)out[3]));
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (i0 + q < M) dst[q] = __longlong_as_double((long long)out[q]);
+                }
+            }
+            // this residue tile may be refilled
+            __syncwarp();
+            if (lane == 0) mbar_arrive(zempty0 + 8 * zb);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
     }
 }
 
@@ -660,27 +702,17 @@ cudaError_t launch_crt_slice(const LeafTask *tasks_dev, int count, int m, SplitP
     return cudaGetLastError();
 }
 
-cudaError_t launch_crt_gemm(const LeafTask *, int count, int m, SplitParams p, void *workspace,
+cudaError_t launch_crt_gemm(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
                             unsigned int *status_dev, int num_sms, cudaStream_t stream) {
     Geo g = make_geo(m, count, p.scheme);
     if (!g.residues_ok) return cudaSuccess;
     cudaError_t e = crt_prepare();
     if (e != cudaSuccess) return e;
-    const int64_t most = (int64_t)g.mtiles * g.rtiles * LMAX * count;  // units, at the most moduli
-    const int grid = (int)(most < num_sms ? most : num_sms);
+    const int64_t units = (int64_t)g.mtiles * g.rtiles * count;
+    int grid = (int)(units < num_sms ? units : num_sms);
+    if (grid > ZCTA_MAX) grid = ZCTA_MAX;  // two product-residue tiles per CTA
     const size_t smem = (size_t)RNSTAGE * RSTAGE_BYTES + 1024 + 1024;
-    crt_gemm_kernel<<<grid, RGEMM_THREADS, smem, stream>>>((char *)workspace, g, status_dev);
-    count_launch();
-    return cudaGetLastError();
-}
-
-cudaError_t launch_split_combine(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
-                                 cudaStream_t stream) {
-    Geo g = make_geo(m, count, p.scheme);
-    if (!g.residues_ok) return cudaSuccess;
-    const int64_t colblocks = (m + 7) / 8;
-    dim3 grid((unsigned)(g.mtiles * colblocks), (unsigned)count);
-    crt_combine_kernel<<<grid, 256, 0, stream>>>(tasks_dev, (char *)workspace, g);
+    crt_gemm_kernel<<<grid, RGEMM_THREADS, smem, stream>>>(tasks_dev, (char *)workspace, g, status_dev);
     count_launch();
     return cudaGetLastError();
 }

@@ -15,6 +15,8 @@ constexpr int MAXS = 8;        // digit scheme: max digits
 constexpr int RTN = 256;       // residue scheme: columns of B per tile (one MMA)
 constexpr int LMAX = 17;       // residue scheme: max moduli
 constexpr int RKMAX = 2048;    // residue scheme: max K (K * 90^2 < 2^24: exact fp32 sums)
+constexpr int ZCTA_MAX = 160;  // residue scheme: GEMM CTAs with product-residue scratch
+constexpr size_t ZTILE_BYTES = (size_t)LMAX * TM * RTN;  // product residues of one tile
 constexpr uint32_t WAIT_LIMIT = 1u << 25;
 
 enum { SCHEME_AUTO = 0, SCHEME_DIGITS = 1, SCHEME_RESIDUES = 2 };
@@ -36,10 +38,11 @@ static_assert(sizeof(SplitHdr) == 256, "split header is 256 bytes");
 
 // Workspace of one launch group of `count` leaves:
 //   [header 256 B][scalars of leaf 0..count-1][plane block of leaf 0..count-1]
+//   [residue scheme: product-residue scratch, two tiles per GEMM CTA]
 // scalars per leaf: f (A rows), g (B columns) of the digit scheme, and the
 // scan's exponent / lsb encodings.  A leaf's plane block holds either the
 // digit planes (A then B, pre-tiled) or, for the residue scheme, the residue
-// planes of A and B and the product residues; it is sized for the larger.
+// planes of A and B; it is sized for the larger.
 struct Geo {
     int m, Mp, Np, Kp, nks, mtiles, ntiles, count;
     int Rp, rtiles;    // residue scheme: B columns padded to 256, and their tiles
@@ -47,7 +50,8 @@ struct Geo {
     size_t sc_per_leaf, dg_per_leaf, sc_base, dg_base, total;
     size_t off_fa, off_fb, off_ea, off_la, off_eb, off_lb;  // within a scalar block
     size_t off_da, off_db;                                  // digit planes
-    size_t off_ra, off_rb, off_ro;                          // residue planes, product residues
+    size_t off_ra, off_rb;                                  // residue planes of A and B
+    size_t z_base;                                          // product-residue scratch
 };
 
 __host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -80,12 +84,12 @@ __host__ __device__ inline Geo make_geo(int m, int count, int scheme) {
     o = 0;
     g.off_ra = o; o += align256((size_t)LMAX * g.Mp * g.Kp * 2);
     g.off_rb = o; o += align256((size_t)LMAX * g.Rp * g.Kp * 2);
-    g.off_ro = o; o += align256((size_t)LMAX * g.Mp * g.Rp);
     const size_t residue_bytes = o;
     g.dg_per_leaf = g.residues_ok && residue_bytes > digits_bytes ? residue_bytes : digits_bytes;
     g.sc_base = 256;
     g.dg_base = 256 + (size_t)count * g.sc_per_leaf;
-    g.total = g.dg_base + (size_t)count * g.dg_per_leaf;
+    g.z_base = g.dg_base + (size_t)count * g.dg_per_leaf;
+    g.total = g.z_base + (g.residues_ok ? (size_t)ZCTA_MAX * 2 * ZTILE_BYTES : 0);
     return g;
 }
 
