@@ -617,14 +617,25 @@ __global__ void __launch_bounds__(RGEMM_THREADS, 1)
 #pragma unroll
             for (int q = 0; q < 4; q++) ei[q] = i0 + q < M ? eap[i0 + q] : 0;
             const unsigned char *zt = ztiles + (size_t)zb * ZTILE_BYTES + lane * 4;
+            // the residue words of column col; the next column's are loaded
+            // before this one is reconstructed (the tiles mostly come from
+            // DRAM: two per CTA exceed L2)
+            uint32_t zq[LMAX], zn[LMAX];
+#pragma unroll
+            for (int l = 0; l < LMAX; l++)
+                zq[l] = l < L ? *reinterpret_cast<const uint32_t *>(zt + ((size_t)l * RTN + w) * TM) : 0u;
 #pragma unroll 1
             for (int col = w; col < RTN; col += 4) {
-                const int64_t j = (int64_t)rt * RTN + col;
-                if (j >= M || i0 >= M) continue;
-                uint32_t zq[LMAX];
+                const int next = col + 4 < RTN ? col + 4 : col;
 #pragma unroll
                 for (int l = 0; l < LMAX; l++)
-                    zq[l] = l < L ? *reinterpret_cast<const uint32_t *>(zt + ((size_t)l * RTN + col) * TM) : 0u;
+                    zn[l] = l < L ? *reinterpret_cast<const uint32_t *>(zt + ((size_t)l * RTN + next) * TM) : 0u;
+                const int64_t j = (int64_t)rt * RTN + col;
+                if (j >= M || i0 >= M) {
+#pragma unroll
+                    for (int l = 0; l < LMAX; l++) zq[l] = zn[l];
+                    continue;
+                }
                 const int ej = ebp[j];
                 int e[4];
                 bool zero[4];
@@ -647,6 +658,8 @@ __global__ void __launch_bounds__(RGEMM_THREADS, 1)
                     for (int q = 0; q < 4; q++)
                         if (i0 + q < M) dst[q] = __longlong_as_double((long long)out[q]);
                 }
+#pragma unroll
+                for (int l = 0; l < LMAX; l++) zq[l] = zn[l];
             }
             // this residue tile may be refilled
             __syncwarp();
