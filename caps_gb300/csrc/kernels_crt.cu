@@ -18,9 +18,10 @@
 //     written as pre-tiled UMMA canonical K-major planes like the digits.
 //  4. gemm:    per modulus, sum_k rA rB on tcgen05.mma kind::f16
 //     (bf16 x bf16 -> f32): |sum| <= K 90^2 < 2^24 for K <= 2048, so the
-//     fp32 accumulator is exact.  Drain warps reduce it modulo p_l and keep
-//     z_l = (c mod p_l) y_l mod p_l, y_l = (M_L / p_l)^-1 mod p_l, one byte
-//     per element, in a product-residue tile of the CTA.
+//     fp32 accumulator is exact.  A's residues are premultiplied by
+//     y_l = (M_L / p_l)^-1 mod p_l, so the sum is y_l A'B' mod p_l; drain
+//     warps reduce it to z_l in [0, p_l), one byte per element, in a
+//     product-residue tile of the CTA.
 //  5. CRT (reconstruction warps of the same kernel, overlapping the next
 //     tile's MMAs): S = sum_l z_l (M_L / p_l) < L M_L is reduced modulo M_L
 //     and centred into (-M_L/2, M_L/2): that is C' exactly; then
@@ -54,8 +55,9 @@ constexpr unsigned RSTATUS = 0x100;               // status bits of this kernel:
 struct CrtTables {
     float p[LMAX], invp[LMAX];
     float c[LMAX][3];              // balanced 2^(14k) mod p_l, k = 1..3
+    float cy[LMAX][LMAX][4];       // [L-1][l][k]: balanced 2^(14k) y_l mod p_l, k = 0..3,
+                                   // y_l = (M_L / p_l)^-1 mod p_l
     int lg[LMAX + 1];              // lg[L] = floor(log2 M_L)
-    float y[LMAX][LMAX];           // [L-1][l]: (M_L / p_l)^-1 mod p_l
     uint32_t Ml[LMAX][LMAX][4];    // [L-1][l]: limbs of M_L / p_l, least significant first
     uint32_t M[LMAX][4];           // [L-1]: limbs of M_L
     float m_inv[LMAX];             // [L-1]: 1 / M_L
@@ -95,12 +97,16 @@ void build_tables(CrtTables &t) {
         t.m_inv[L - 1] = (float)(1.0 / (double)M);
         for (int l = 0; l < LMAX; l++) {
             if (l >= L) {
-                t.y[L - 1][l] = 0.0f;
-                for (int k = 0; k < 4; k++) t.Ml[L - 1][l][k] = 0;
+                for (int k = 0; k < 4; k++) t.Ml[L - 1][l][k] = t.cy[L - 1][l][k] = 0;
                 continue;
             }
             const u128 Ml = M / (u128)MODULI[l];
-            t.y[L - 1][l] = (float)mod_inverse((int)(Ml % (u128)MODULI[l]), MODULI[l]);
+            const int p = MODULI[l], y = mod_inverse((int)(Ml % (u128)p), p);
+            long long v = y;
+            for (int k = 0; k < 4; k++) {
+                t.cy[L - 1][l][k] = (float)(v > p / 2 ? v - p : v);
+                v = (v * 16384) % p;
+            }
             for (int k = 0; k < 4; k++) t.Ml[L - 1][l][k] = (uint32_t)(Ml >> (32 * k));
         }
     }
@@ -152,6 +158,18 @@ __device__ __forceinline__ Limbs limbs14(long long X) {
 // the balanced residue of x's integer modulo p_l, as an fp32 value (|r| <= 90)
 __device__ __forceinline__ float residue_f32(const Limbs &x, int l) {
     const float y = fmaf(x.a[3], c_crt.c[l][2], fmaf(x.a[2], c_crt.c[l][1], fmaf(x.a[1], c_crt.c[l][0], x.a[0])));
+    const float q = fmaf(y, c_crt.invp[l], MAGIC) - MAGIC;
+    return fmaf(-q, c_crt.p[l], y);
+}
+
+// the same for x's integer times y_l (the CRT coefficient of modulus l among
+// L): A's residues carry y_l, so each modulus's product sum is already
+// y_l A'B' mod p_l, the term the CRT needs.  |y| <= 4 * 8192 * 90 < 2^21.5,
+// so y / p is within 2^-9.3 of y * fl(1/p), still inside the half-integer
+// margin of 2^-8.5.
+__device__ __forceinline__ float residue_y_f32(const Limbs &x, int L, int l) {
+    const float *cy = c_crt.cy[L - 1][l];
+    const float y = fmaf(x.a[3], cy[3], fmaf(x.a[2], cy[2], fmaf(x.a[1], cy[1], x.a[0] * cy[0])));
     const float q = fmaf(y, c_crt.invp[l], MAGIC) - MAGIC;
     return fmaf(-q, c_crt.p[l], y);
 }
@@ -253,12 +271,23 @@ __global__ void __launch_bounds__(256) crt_slice_kernel(const LeafTask *__restri
     Limbs x[8];
 #pragma unroll
     for (int e = 0; e < 8; e++) x[e] = limbs14(scaled_round(v[e], f));
+    if (blockIdx.y == 0) {
 #pragma unroll 1
-    for (int l = 0; l < L; l++) {
-        uint32_t w[4];
+        for (int l = 0; l < L; l++) {
+            uint32_t w[4];
 #pragma unroll
-        for (int q = 0; q < 4; q++) w[q] = pack_bf16x2(residue_f32(x[2 * q], l), residue_f32(x[2 * q + 1], l));
-        *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
+            for (int q = 0; q < 4; q++)
+                w[q] = pack_bf16x2(residue_y_f32(x[2 * q], L, l), residue_y_f32(x[2 * q + 1], L, l));
+            *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+    } else {
+#pragma unroll 1
+        for (int l = 0; l < L; l++) {
+            uint32_t w[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) w[q] = pack_bf16x2(residue_f32(x[2 * q], l), residue_f32(x[2 * q + 1], l));
+            *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
     }
 }
 
@@ -562,7 +591,7 @@ __global__ void __launch_bounds__(RGEMM_THREADS, 1)
                 const bool got = mbar_wait(tfull0 + 8 * acc, (uc >> 1) & 1, status, RSTATUS << 5);
                 if (!__all_sync(0xffffffffu, got)) { ok = false; break; }
                 tc_fence_after();
-                const float p = c_crt.p[l], invp = c_crt.invp[l], y = c_crt.y[L - 1][l];
+                const float p = c_crt.p[l], invp = c_crt.invp[l];
                 unsigned char *out = zt + (size_t)l * RTN * TM;
 #pragma unroll 1
                 for (int c4 = 0; c4 < 4; c4++) {
@@ -571,16 +600,12 @@ __global__ void __launch_bounds__(RGEMM_THREADS, 1)
                     tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + acc * RTN + col0, v);
 #pragma unroll
                     for (int e = 0; e < 32; e++) {
-                        // c = sum rA rB (exact, |c| < 2^24).  q = c / p rounded
-                        // by MAGIC is floor or ceil of c / p (|c / p| 2^-24 < 1/2
-                        // away), so c - q p lies in [-p, p) and one correction
-                        // gives r = c mod p in [0, p).
+                        // c = sum rA rB = y A'B' mod p (exact, |c| < 2^24; A's
+                        // residues carry y).  q = c / p rounded by MAGIC is floor
+                        // or ceil of c / p (|c / p| 2^-24 < 1/2 away), so c - q p
+                        // lies in [-p, p) and one correction gives z = c mod p.
                         const float c = __uint_as_float(v[e]);
-                        float r = fmaf(-(fmaf(c, invp, MAGIC) - MAGIC), p, c);
-                        r = r < 0.0f ? r + p : r;
-                        // z = r y mod p, the same way (r y < 2^15, exact)
-                        const float ry = r * y;
-                        float z = fmaf(-(fmaf(ry, invp, MAGIC) - MAGIC), p, ry);
+                        float z = fmaf(-(fmaf(c, invp, MAGIC) - MAGIC), p, c);
                         z = z < 0.0f ? z + p : z;
                         out[(size_t)(col0 + e) * TM] = (unsigned char)__float_as_uint(z + MAGIC);  // low byte: z
                     }
