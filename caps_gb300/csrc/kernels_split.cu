@@ -555,6 +555,9 @@ cudaError_t launch_split_prep(const LeafTask *tasks_dev, int count, int m, Split
     if (e != cudaSuccess) return e;
     e = launch_crt_slice(tasks_dev, count, m, p, ws, stream);
     if (e != cudaSuccess) return e;
+    // a forced residue scheme always runs when the leaves fit it (L <= 17 for
+    // 55-bit operands and K <= 2048): the digit kernels need no launch
+    if (p.scheme == SCHEME_RESIDUES && g.residues_ok) return cudaSuccess;
     {
         int64_t atiles = (int64_t)g.mtiles * g.nks;
         int64_t btiles2 = ((int64_t)g.ntiles * g.nks + 1) / 2;
@@ -575,12 +578,14 @@ cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, Split
     const size_t smem = (size_t)NSTAGE * STAGE_BYTES + 1024 + 1024;
     e = g_prepare_error;
     if (e != cudaSuccess) return e;
-    int64_t total = (int64_t)g.mtiles * g.ntiles * count;
-    int grid = (int)(total < g_num_sms ? total : g_num_sms);
-    split_gemm_kernel<<<grid, GEMM_THREADS, smem, stream>>>(tasks_dev, count, ws, g, p, status_dev);
-    count_launch();
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    if (!(p.scheme == SCHEME_RESIDUES && g.residues_ok)) {  // see launch_split_prep
+        int64_t total = (int64_t)g.mtiles * g.ntiles * count;
+        int grid = (int)(total < g_num_sms ? total : g_num_sms);
+        split_gemm_kernel<<<grid, GEMM_THREADS, smem, stream>>>(tasks_dev, count, ws, g, p, status_dev);
+        count_launch();
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
     return launch_crt_gemm(tasks_dev, count, m, p, ws, status_dev, g_num_sms, stream);
 }
 
