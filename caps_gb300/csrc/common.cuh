@@ -111,8 +111,6 @@ size_t split_workspace_bytes(int m, int count, int scheme);
 // Computes per-row / per-column scale exponents and the needed digit count.
 cudaError_t launch_split_scan(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
                              cudaStream_t stream);
-// Reads back the digits needed (max over the batch) from the scan results.
-cudaError_t split_needed_slices(void *workspace, int count, int m, int *needed, cudaStream_t stream);
 // Exponents, the scheme choice, and the operand slices (digit or residue planes).
 cudaError_t launch_split_prep(const LeafTask *tasks_dev, int count, int m, SplitParams p,
                               void *workspace, cudaStream_t stream);

@@ -787,7 +787,10 @@ static int64_t batch_ws_per_instance(int n, int nrec, const char *pat, int form,
         if (pat[k] == 'b' || pat[k] == 'B') count *= 7;
         m /= 2;
     }
-    if (form == CAPS_FORM_SPLIT) total += (int64_t)split_workspace_bytes((int)m, (int)count, scheme);
+    // the split scratch's per-leaf bytes (its fixed part is counted once per launch group)
+    if (form == CAPS_FORM_SPLIT)
+        total += (int64_t)(split_workspace_bytes((int)m, (int)(2 * count), scheme) -
+                           split_workspace_bytes((int)m, (int)count, scheme));
     return total;
 }
 

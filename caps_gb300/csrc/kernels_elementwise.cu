@@ -13,9 +13,6 @@
 
 namespace caps {
 
-template <int OP, typename V>
-struct EwBody;
-
 // Winograd operand sums (reference order, multiply.cpp:421-435):
 //   S5 = B22-B12; S3 = B12-B11; S4 = B22-S3; T3 = A21+A22; T5 = A11-A21;
 //   T4 = T3-A11;  T6 = A12-T4;  S7 = S4-B21.

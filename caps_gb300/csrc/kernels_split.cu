@@ -589,13 +589,4 @@ cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, Split
     return launch_crt_gemm(tasks_dev, count, m, p, ws, status_dev, g_num_sms, stream);
 }
 
-cudaError_t split_needed_slices(void *workspace, int, int, int *needed, cudaStream_t stream) {
-    SplitHdr h;
-    cudaError_t e = cudaMemcpyAsync(&h, workspace, sizeof(int) * 3, cudaMemcpyDeviceToHost, stream);
-    if (e != cudaSuccess) return e;
-    e = cudaStreamSynchronize(stream);
-    if (needed) *needed = h.needed;
-    return e;
-}
-
 }  // namespace caps
