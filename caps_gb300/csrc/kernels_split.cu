@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(256) split_scan_kernel(const LeafTask *__restr
 #pragma unroll 8
         for (int64_t k = k0; k < k1; k++) {
             double x = __ldg(t.A + i + k * M);
-            if (x != 0.0) {
+            if ((unsigned long long)__double_as_longlong(x) << 1) {  // x != 0 by its encoding (an FP64 compare runs at 1/64 rate)
                 int E, lb;
                 exp_lsb(x, E, lb);
                 emax = E > emax ? E : emax;
@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(256) split_scan_kernel(const LeafTask *__restr
 #pragma unroll 8
         for (int64_t k = lane; k < M; k += 32) {
             double x = __ldg(t.B + k + j * M);
-            if (x != 0.0) {
+            if ((unsigned long long)__double_as_longlong(x) << 1) {  // x != 0 by its encoding
                 int E, lb;
                 exp_lsb(x, E, lb);
                 emax = E > emax ? E : emax;
