@@ -60,8 +60,9 @@ class MatDescriptor(ctypes.Structure):
                 ("bs", ctypes.c_int)]
 
     @classmethod
-    def make(cls, lda: int, nrec: int, bs: int = 1) -> "MatDescriptor":
-        return cls(lda, nrec, 1, 1, 1, 1, bs)
+    def make(cls, lda: int, nrec: int, bs: int = 1, hybrid: int = 1) -> "MatDescriptor":
+        """hybrid: subproducts an 'h' step runs at once (the nproc_summa field)."""
+        return cls(lda, nrec, 1, 1, 1, int(hybrid), bs)
 
 
 class Options(ctypes.Structure):

@@ -151,6 +151,7 @@ struct Builder {
     long long adds = 0, muls = 0, add_bytes = 0;
     int split_group = 0;
     bool host_overlap = false;  // emit K_WAIT / K_RECORD at the top-level 'd' step
+    int hybrid = 1;             // subproducts an 'h' step runs at once (desc.nproc_summa)
 
     size_t mark() const { return top; }
     void release(size_t m) { top = m; }
@@ -313,11 +314,17 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
     b.adds += 15LL * q * (long long)P.size();
     size_t mk = b.mark();
     std::vector<EwTask> st(P.size());
-    if (c == 'b' || c == 'B') {
+    const bool hyb = (c == 'h' || c == 'H') && b.hybrid >= 2;
+    if (c == 'b' || c == 'B' || hyb) {
         // strassenBFS (multiply.cpp:212-310) on one GPU: 7 subproducts as one
         // batch.  Q1..Q4 are written straight into the C quadrants (calcCij
         // reads all seven products of an element before writing any of its
         // four results), Q5..Q7 into workspace: 11 quarter buffers per node.
+        // A hybrid step with factor k (strassenHybrid2..6, multiply.cpp:458-1080,
+        // which run k subproducts on k process groups at once) forms the same
+        // operands and combines the same products, but runs the subproducts
+        // through the levels below k at a time, so only k of them hold
+        // workspace at once.
         std::vector<Prob> ch;
         std::vector<EwTask> cij(P.size());
         for (size_t i = 0; i < P.size(); i++) {
@@ -346,7 +353,17 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
             cij[i] = t;
         }
         emit_ew(b, EW_FORM_ST, st, q);
-        build(b, ch, h, nrec - 1, pat + 1);
+        if (!hyb) {
+            build(b, ch, h, nrec - 1, pat + 1);
+        } else {
+            // subproducts k at a time; ch holds them node by node, 7 per node
+            for (int s0 = 0; s0 < 7; s0 += b.hybrid) {
+                std::vector<Prob> part;
+                for (size_t i = 0; i < P.size(); i++)
+                    for (int k = s0; k < s0 + b.hybrid && k < 7; k++) part.push_back(ch[i * 7 + k]);
+                build(b, part, h, nrec - 1, pat + 1);
+            }
+        }
         emit_ew(b, EW_CALC_CIJ, cij, q);
     } else {
         // strassenDFS (multiply.cpp:409-454), memory-lean: each operand pair
@@ -428,8 +445,13 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
 }
 
 // ------------------------------------------------------------------ checks
+// nproc_summa is the reference's P factor, the process groups a hybrid step
+// spreads its subproducts over; on one GPU it is the number of subproducts an
+// 'h' step runs at once (1: the step runs as 'd', as the reference does on one
+// rank; 2..6: strassenHybrid2..6's split; other values are rejected, as
+// multiply.cpp:92-96 rejects them).
 static caps_status check_desc(const caps_desc &d) {
-    if (d.nproc != 1 || d.nprocr != 1 || d.nprocc != 1 || d.nproc_summa != 1)
+    if (d.nproc != 1 || d.nprocr != 1 || d.nprocc != 1 || d.nproc_summa < 1 || d.nproc_summa > 6)
         return CAPS_ERR_UNSUPPORTED;
     if (d.lda <= 0 || d.nrec < 0 || d.bs <= 0 || d.nrec > 24) return CAPS_ERR_SIZE;
     int64_t unit = ((int64_t)1 << d.nrec) * d.bs;
@@ -510,6 +532,7 @@ static caps_status plan(const double *A, const double *B, double *C, const caps_
     pl.b.host_overlap = host_overlap;
     pl.b.ws_base = ws_base;
     pl.b.bs = d.bs;
+    pl.b.hybrid = d.nproc_summa;
     pl.b.opt = o;
     std::vector<Prob> P{{A, B, C}};
     build(pl.b, P, d.lda, d.nrec, pat);
@@ -1062,7 +1085,10 @@ caps_status caps_multiply_host(const double *A, const double *B, double *C, caps
         auto_pattern(desc, o, pat);
         if (desc.nrec > 0) pat[0] = 'd';  // the lean top step lets the copies overlap
     }
-    const bool overlap = desc.nrec > 0 && (pat[0] == 'd' || pat[0] == 'D' || pat[0] == 'h' || pat[0] == 'H');
+    // the lean 'd' step (and 'h' with factor 1, which runs as 'd') waits on the
+    // copies quadrant by quadrant; other top steps take the copies whole
+    const bool overlap = desc.nrec > 0 && (pat[0] == 'd' || pat[0] == 'D' ||
+                                           ((pat[0] == 'h' || pat[0] == 'H') && desc.nproc_summa == 1));
     size_t nn = (size_t)desc.lda * desc.lda * sizeof(double);
     size_t slot = (nn + 255) & ~(size_t)255;
     CAPS_TRY(ensure(g_io, 3 * slot));

@@ -27,7 +27,11 @@ typedef struct caps_desc {
     int nproc;        /* must be 1: one GPU holds the whole matrix */
     int nprocr;       /* must be 1 */
     int nprocc;       /* must be 1 */
-    int nproc_summa;  /* must be 1 */
+    int nproc_summa;  /* the reference's P factor (process groups of a hybrid
+                         'h' step); on one GPU, the subproducts an 'h' step runs at
+                         once: 1 (the step runs as 'd', as the reference does on
+                         one rank) or 2..6 (strassenHybrid2..6, multiply.cpp:458-1080:
+                         the operands of a 'b' step, its subproducts k at a time) */
     int bs;           /* leaf block size; lda % (2^nrec * bs) == 0 */
 } caps_desc;
 

@@ -244,3 +244,41 @@ def test_fromfile1_on_generated_fixture(caps, cuda, tmp_path):
             out = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=120)
             assert out.returncode == 0, out.stdout
             assert "Maximum deviation 0.000000e+00" in out.stdout, (bs, r, form, out.stdout)
+
+
+@pytest.mark.parametrize("pat,k,ref_pat", [("hhh", 2, "bbb"), ("hhh", 3, "bbb"), ("hhh", 6, "bbb"),
+                                           ("hbd", 4, "bbd"), ("hhh", 1, "ddd")])
+def test_hybrid_steps_match_bfs_and_dfs_bit_for_bit(caps, oracle_mod, cuda, pat, k, ref_pat):
+    """strassenHybrid2..6 (multiply.cpp:458-1080) form a 'b' step's operands and
+    combine its products, running the subproducts k at a time; factor 1 runs
+    the step as 'd'.  Per element the arithmetic is the same, so the results
+    are bit-identical on float data."""
+    import torch
+    n, r = 1024, 3
+    rng = np.random.default_rng(40 + k)
+    A = rng.uniform(-1, 1, (n, n))
+    B = rng.uniform(-1, 1, (n, n))
+    dA = torch.from_numpy(caps_of(oracle_mod, A, r)).to(cuda)
+    dB = torch.from_numpy(caps_of(oracle_mod, B, r)).to(cuda)
+    out = {}
+    for key, p, kk in (("h", pat, k), ("ref", ref_pat, 1)):
+        dC = torch.full_like(dA, float("nan"))
+        caps.multiply(dA, dB, dC, caps.MatDescriptor.make(n, r, 1, kk), p, form="plain")
+        torch.cuda.synchronize()
+        out[key] = dC.cpu().numpy()
+    assert np.array_equal(out["h"], out["ref"])
+
+
+def test_hybrid_split_integers_exact(caps, oracle_mod, cuda):
+    import torch
+    n, r = 896, 2
+    rng = np.random.default_rng(3)
+    A = rng.integers(-50, 51, (n, n)).astype(np.float64)
+    B = rng.integers(-50, 51, (n, n)).astype(np.float64)
+    dA = torch.from_numpy(caps_of(oracle_mod, A, r)).to(cuda)
+    dB = torch.from_numpy(caps_of(oracle_mod, B, r)).to(cuda)
+    dC = torch.full_like(dA, float("nan"))
+    caps.multiply(dA, dB, dC, caps.MatDescriptor.make(n, r, 1, 3), "hh", form="split")
+    torch.cuda.synchronize()
+    C = mat_of(oracle_mod, dC.cpu().numpy(), n, r)
+    assert np.array_equal(C, (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64))

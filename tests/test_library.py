@@ -101,3 +101,23 @@ def test_reference_drivers_link_unmodified_against_library(caps, tmp_path):
                "-Wl,-rpath," + libdir]
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
         assert r.returncode == 0, r.stdout
+
+
+def test_hybrid_step_workspace_between_d_and_b(caps):
+    """An 'h' step with factor k (desc.nproc_summa) holds the workspace of k
+    concurrent subproducts: more than 'd', less than 'b'; k = 1 runs as 'd'."""
+    n = 16384
+
+    def ws(pat, k=1):
+        return caps.workspace_size(caps.MatDescriptor.make(n, len(pat), 1, k), pat, form="plain")
+
+    assert ws("hhh", 1) == ws("ddd")
+    sizes = [ws("ddd")] + [ws("hhh", k) for k in (2, 3, 4, 5, 6)] + [ws("bbb")]
+    assert sizes == sorted(sizes) and len(set(sizes)) == len(sizes), sizes
+
+
+def test_hybrid_factor_outside_reference_range_rejected(caps):
+    for k in (0, 7):
+        with pytest.raises(caps.CapsError) as e:
+            caps.workspace_size(caps.MatDescriptor.make(1024, 2, 1, k), "hh")
+        assert e.value.status == 7  # CAPS_ERR_UNSUPPORTED
