@@ -282,3 +282,18 @@ def test_hybrid_split_integers_exact(caps, oracle_mod, cuda):
     torch.cuda.synchronize()
     C = mat_of(oracle_mod, dC.cpu().numpy(), n, r)
     assert np.array_equal(C, (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64))
+
+
+@pytest.mark.parametrize("k", [1, 2, 5])
+def test_host_entry_hybrid_top_step(caps, oracle_mod, cuda, k):
+    """Host arrays with a top-level 'h' step: factor 1 runs it as 'd' with the
+    copies overlapped; factors 2..6 take the copies whole before the step."""
+    n, r = 512, 3
+    rng = np.random.default_rng(20 + k)
+    A = rng.integers(-100, 101, (n, n)).astype(np.float64)
+    B = rng.integers(-100, 101, (n, n)).astype(np.float64)
+    a, b = caps_of(oracle_mod, A, r), caps_of(oracle_mod, B, r)
+    for form in ("plain", "split"):
+        c = np.full(n * n, np.nan)
+        caps.multiply(a, b, c, caps.MatDescriptor.make(n, r, 1, k), "hbd", form=form)
+        assert np.array_equal(mat_of(oracle_mod, c, n, r), (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64))
