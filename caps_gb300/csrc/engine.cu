@@ -113,10 +113,12 @@ static caps_status pinned_reserve(size_t bytes) {
 enum OpKind { K_EW = 0, K_LEAF_DMMA, K_LEAF_SPLIT, K_REORDER, K_WAIT, K_RECORD };
 
 // Events the host entry point uses to overlap its copies with a top-level
-// 'd' step: the step waits for A11/B11 (0) before Q1 and for the other input
-// quadrants (1) before forming T4/S4; it records when C22 (2), C21 (3) and
-// C12 (4) are final so their copies back run under the later subproducts.
-constexpr int HOST_EVENTS = 5;
+// 'd' step: the step waits for A11/B11 (0) before Q1, for A12/B21 (1) before
+// Q2 and for the other input quadrants (2) before forming T4/S4; it records
+// when C11 (3), C22 (4), C21 (5) and C12 (6) are final so their copies back
+// run under the later subproducts.
+constexpr int HOST_EVENTS = 7;
+constexpr int EV_C_FIRST = 3;  // events 3..6: C11, C22, C21, C12 final
 enum Phase { PH_ADD = 0, PH_MUL = 1, PH_REARRANGE = 2 };
 
 struct Op {
@@ -416,30 +418,46 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
             }
             emit_ew(b, op, t, q);
         };
+        // At the top of a host call the inputs arrive quadrant by quadrant:
+        // Q1 = A11 B11 and Q2 = A12 B21 run first (Q2 into a buffer of its
+        // own) while the rest is copied, and C11 = Q1 + Q2 is final as soon as
+        // U1 = C11 + Q4 has read Q1 -- the same sums as below, where Q2 comes
+        // last to save the buffer.
         const bool top = b.host_overlap && P.size() == 1 && b.ops.empty();
+        double *Q2top = top ? b.alloc(q) : nullptr;
         if (top) emit_event(b, K_WAIT, 0);  // A11, B11 on the device
         sub(1);
-        if (top) emit_event(b, K_WAIT, 1);  // the other six input quadrants
+        if (top) {
+            emit_event(b, K_WAIT, 1);  // A12, B21
+            build(b, {{nd[0].A12, nd[0].B21, Q2top}}, h, nrec - 1, pat + 1);
+            emit_event(b, K_WAIT, 2);  // A21, A22, B11, B12, B22
+        }
         form(EW_FORM_T4S4);
         sub(4);
         comb(EW_ADD_DUP, [](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = d.Q; t.dst[0] = d.C22; t.dst[1] = d.C12; });
+        if (top) {
+            comb(EW_ADD, [&](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = Q2top; t.dst[0] = d.C11; });
+            emit_event(b, K_RECORD, EV_C_FIRST);  // C11 final
+        }
         form(EW_FORM_T5S5);
         sub(5);
         comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C22; t.src[1] = d.Q; t.dst[0] = d.C22; });
         form(EW_FORM_T3S3);
         sub(3);
         comb(EW_U2_Q3, [](const Nd &d, EwTask &t) { t.src[0] = d.C22; t.src[1] = d.C12; t.src[2] = d.Q; t.dst[0] = d.C21; t.dst[1] = d.C22; t.dst[2] = d.C12; });
-        if (top) emit_event(b, K_RECORD, 2);  // C22 final
+        if (top) emit_event(b, K_RECORD, EV_C_FIRST + 1);  // C22 final
         form(EW_FORM_S7);
         sub(7);
         comb(EW_SUB, [](const Nd &d, EwTask &t) { t.src[0] = d.C21; t.src[1] = d.Q; t.dst[0] = d.C21; });
-        if (top) emit_event(b, K_RECORD, 3);  // C21 final
+        if (top) emit_event(b, K_RECORD, EV_C_FIRST + 2);  // C21 final
         form(EW_FORM_T6);
         sub(6);
         comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C12; t.src[1] = d.Q; t.dst[0] = d.C12; });
-        if (top) emit_event(b, K_RECORD, 4);  // C12 final
-        sub(2);
-        comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = d.Q; t.dst[0] = d.C11; });
+        if (top) emit_event(b, K_RECORD, EV_C_FIRST + 3);  // C12 final
+        if (!top) {
+            sub(2);
+            comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = d.Q; t.dst[0] = d.C11; });
+        }
     }
     b.release(mk);
 }
@@ -1116,27 +1134,31 @@ caps_status caps_multiply_host(const double *A, const double *B, double *C, caps
     };
     CAPS_CUDA_TRY(cudaEventRecord(start, s));  // after earlier work on s
     CAPS_CUDA_TRY(cudaStreamWaitEvent(cs, start, 0));
+    // quadrants X11, X21, X12, X22 at 0, q, 2q, 3q: A11 + B11 (Q1), then
+    // A12 + B21 (Q2), then the rest
     CAPS_CUDA_TRY(h2d(dA, A, 0));
     CAPS_CUDA_TRY(h2d(dB, B, 0));
     CAPS_CUDA_TRY(cudaEventRecord(g_host_events[0], cs));
-    for (int quad = 1; quad < 4; quad++) {
-        CAPS_CUDA_TRY(h2d(dA, A, quad));
-        CAPS_CUDA_TRY(h2d(dB, B, quad));
-    }
+    CAPS_CUDA_TRY(h2d(dA, A, 2));
+    CAPS_CUDA_TRY(h2d(dB, B, 1));
     CAPS_CUDA_TRY(cudaEventRecord(g_host_events[1], cs));
+    CAPS_CUDA_TRY(h2d(dA, A, 1));
+    CAPS_CUDA_TRY(h2d(dA, A, 3));
+    CAPS_CUDA_TRY(h2d(dB, B, 2));
+    CAPS_CUDA_TRY(h2d(dB, B, 3));
+    CAPS_CUDA_TRY(cudaEventRecord(g_host_events[2], cs));
     caps_status st = multiply_dev_locked(dA, dB, dC, desc, pat, o, s, false, true);
     if (st != CAPS_OK) {
         cudaStreamSynchronize(cs);
         return st;
     }
-    // C22 (quadrant 3), C21 (1), C12 (2) as they become final, C11 (0) at the end
-    const int quad_of_event[5] = {-1, -1, 3, 1, 2};
-    for (int e = 2; e < HOST_EVENTS; e++) {
+    // C11 (quadrant 0), C22 (3), C21 (1), C12 (2) as they become final
+    const int quad_of_event[HOST_EVENTS - EV_C_FIRST] = {0, 3, 1, 2};
+    for (int e = EV_C_FIRST; e < HOST_EVENTS; e++) {
         CAPS_CUDA_TRY(cudaStreamWaitEvent(cs, g_host_events[e], 0));
-        int quad = quad_of_event[e];
+        const int quad = quad_of_event[e - EV_C_FIRST];
         CAPS_CUDA_TRY(cudaMemcpyAsync((char *)C + quad * q, (char *)dC + quad * q, q, cudaMemcpyDeviceToHost, cs));
     }
-    CAPS_CUDA_TRY(cudaMemcpyAsync(C, dC, q, cudaMemcpyDeviceToHost, s));
     if (o.form == CAPS_FORM_SPLIT) CAPS_TRY(check_device_status(s, nullptr));
     CAPS_CUDA_TRY(cudaStreamSynchronize(s));
     CAPS_CUDA_TRY(cudaStreamSynchronize(cs));
