@@ -216,24 +216,21 @@ __global__ void crt_resolve_kernel(char *__restrict__ ws, Geo g, SplitParams p) 
 //   matrices, K halves side by side: K stride 128 B, row-group stride 256 B).
 // A side: one thread = one row x 8 k, a block = one 128 x 16 tile.  B side:
 // one thread = one column x 8 k, a block = half of a 256 x 16 tile.
-__global__ void __launch_bounds__(256) crt_slice_kernel(const LeafTask *__restrict__ tasks,
-                                                        char *__restrict__ ws, Geo g) {
-    const SplitHdr *h = reinterpret_cast<const SplitHdr *>(ws);
-    if (!h->residues) return;  // the digit scheme runs
-    const int L = h->moduli;
-    const LeafTask t = tasks[blockIdx.z];
-    const char *sc = leaf_scalars(ws, g, blockIdx.z);
-    char *pl = leaf_digits(ws, g, blockIdx.z);
+__device__ __forceinline__ void crt_slice_tile(const LeafTask *__restrict__ tasks, char *__restrict__ ws,
+                                               const Geo &g, const SplitHdr *h, int L, int leaf, int64_t tile,
+                                               int side) {
+    const LeafTask t = tasks[leaf];
+    const char *sc = leaf_scalars(ws, g, leaf);
+    char *pl = leaf_digits(ws, g, leaf);
     const int64_t M = g.m;
     const int tid = threadIdx.x;
-    const int64_t tile = blockIdx.x;
     const int kg = tid >> 7;  // which 8 of the tile's 16 k
     int64_t idx, k0, sk;      // row of A / column of B, first k, stride between k
     const double *src;
     int ee, tt;
     char *dst;
     size_t plane_stride;
-    if (blockIdx.y == 0) {
+    if (side == 0) {
         if (tile >= (int64_t)g.mtiles * g.nks) return;
         const int mt = (int)(tile / g.nks), ks = (int)(tile % g.nks);
         const int r = tid & 127;
@@ -271,7 +268,7 @@ __global__ void __launch_bounds__(256) crt_slice_kernel(const LeafTask *__restri
     Limbs x[8];
 #pragma unroll
     for (int e = 0; e < 8; e++) x[e] = limbs14(scaled_round(v[e], f));
-    if (blockIdx.y == 0) {
+    if (side == 0) {
 #pragma unroll 1
         for (int l = 0; l < L; l++) {
             uint32_t w[4];
@@ -289,6 +286,20 @@ __global__ void __launch_bounds__(256) crt_slice_kernel(const LeafTask *__restri
             *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
         }
     }
+}
+
+// Grid-stride over (leaf, tile), so that the launch is cheap when the digit
+// scheme runs and this kernel returns at once.  blockIdx.y: A (0) or B (1).
+__global__ void __launch_bounds__(256) crt_slice_kernel(const LeafTask *__restrict__ tasks,
+                                                        char *__restrict__ ws, Geo g) {
+    const SplitHdr *h = reinterpret_cast<const SplitHdr *>(ws);
+    if (!h->residues) return;  // the digit scheme runs
+    const int L = h->moduli;
+    const int64_t atiles = (int64_t)g.mtiles * g.nks, bhalves = (int64_t)g.rtiles * g.nks * 2;
+    const int64_t per = atiles > bhalves ? atiles : bhalves;
+    const int64_t total = per * g.count;
+    for (int64_t it = blockIdx.x; it < total; it += gridDim.x)
+        crt_slice_tile(tasks, ws, g, h, L, (int)(it / per), it % per, blockIdx.y);
 }
 
 // ---------------------------------------------------------------- CRT reconstruction
@@ -734,7 +745,8 @@ cudaError_t launch_crt_slice(const LeafTask *tasks_dev, int count, int m, SplitP
     Geo g = make_geo(m, count, p.scheme);
     if (!g.residues_ok) return cudaSuccess;
     const int64_t atiles = (int64_t)g.mtiles * g.nks, bhalves = (int64_t)g.rtiles * g.nks * 2;
-    dim3 grid((unsigned)(atiles > bhalves ? atiles : bhalves), 2, (unsigned)count);
+    const int64_t items = (atiles > bhalves ? atiles : bhalves) * count;
+    dim3 grid((unsigned)(items < 4096 ? items : 4096), 2);
     crt_slice_kernel<<<grid, 256, 0, stream>>>(tasks_dev, (char *)workspace, g);
     count_launch();
     return cudaGetLastError();

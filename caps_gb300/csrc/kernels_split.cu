@@ -185,19 +185,15 @@ __device__ __forceinline__ uint32_t bf16_of_digit(int d) {
 // A side: one thread = one row x 8 k (16 bytes per plane); 256 threads = one
 // 128 x 16 tile.  B side: one thread = one column x 8 k; 256 threads = two
 // 64 x 16 tiles.
-__global__ void __launch_bounds__(256) split_slice_kernel(const LeafTask *__restrict__ tasks, int m,
-                                                          char *__restrict__ ws, Geo g, SplitParams p) {
-    if (reinterpret_cast<const SplitHdr *>(ws)->residues) return;  // the residue scheme runs
-    const LeafTask t = tasks[blockIdx.z];
-    char *sc = leaf_scalars(ws, g, blockIdx.z);
-    char *dg = leaf_digits(ws, g, blockIdx.z);
-    int s, nd;
-    resolve_sd(reinterpret_cast<const SplitHdr *>(ws), p, s, nd);
+__device__ __forceinline__ void split_slice_tile(const LeafTask *__restrict__ tasks, int m, char *__restrict__ ws,
+                                                 const Geo &g, int s, int leaf, int64_t tile, int side) {
+    const LeafTask t = tasks[leaf];
+    char *sc = leaf_scalars(ws, g, leaf);
+    char *dg = leaf_digits(ws, g, leaf);
     const int64_t M = m;
     const int tid = threadIdx.x;
-    int64_t tile = blockIdx.x;
     const int64_t atiles = (int64_t)g.mtiles * g.nks;
-    if (blockIdx.y == 0) {
+    if (side == 0) {
         if (tile >= atiles) return;
         int mt = (int)(tile / g.nks), ks = (int)(tile % g.nks);
         int r = tid & 127, kg = tid >> 7;
@@ -254,6 +250,21 @@ __global__ void __launch_bounds__(256) split_slice_kernel(const LeafTask *__rest
                 make_uint4(packed[pl][0], packed[pl][1], packed[pl][2], packed[pl][3]);
         }
     }
+}
+
+// Grid-stride over (leaf, tile), so that the launch is cheap when the residue
+// scheme runs and this kernel returns at once.  blockIdx.y: A (0) or B (1).
+__global__ void __launch_bounds__(256) split_slice_kernel(const LeafTask *__restrict__ tasks, int m,
+                                                          char *__restrict__ ws, Geo g, SplitParams p) {
+    const SplitHdr *h = reinterpret_cast<const SplitHdr *>(ws);
+    if (h->residues) return;  // the residue scheme runs
+    int s, nd;
+    resolve_sd(h, p, s, nd);
+    const int64_t atiles = (int64_t)g.mtiles * g.nks, btiles2 = ((int64_t)g.ntiles * g.nks + 1) / 2;
+    const int64_t per = atiles > btiles2 ? atiles : btiles2;
+    const int64_t total = per * g.count;
+    for (int64_t it = blockIdx.x; it < total; it += gridDim.x)
+        split_slice_tile(tasks, m, ws, g, s, (int)(it / per), it % per, blockIdx.y);
 }
 
 // ---------------------------------------------------------------- gemm
@@ -561,8 +572,8 @@ cudaError_t launch_split_prep(const LeafTask *tasks_dev, int count, int m, Split
     {
         int64_t atiles = (int64_t)g.mtiles * g.nks;
         int64_t btiles2 = ((int64_t)g.ntiles * g.nks + 1) / 2;
-        int64_t gx = atiles > btiles2 ? atiles : btiles2;
-        dim3 grid((unsigned)gx, 2, (unsigned)count);
+        int64_t items = (atiles > btiles2 ? atiles : btiles2) * count;
+        dim3 grid((unsigned)(items < 4096 ? items : 4096), 2);
         split_slice_kernel<<<grid, 256, 0, stream>>>(tasks_dev, m, ws, g, p);
         count_launch();
     }
