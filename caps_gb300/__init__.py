@@ -42,7 +42,7 @@ C_ABI_SYMBOLS = [
     "caps_from_caps_layout_dev", "caps_leaf_gemm_dev", "caps_workspace_size", "caps_resolve_pattern",
     "caps_get_counters", "caps_reset_counters", "caps_set_phase_timing", "caps_multiply_batched_dev",
     "caps_status_string", "caps_last_cuda_error", "caps_debug_fail_allocations", "caps_release_cache",
-    "caps_leaf_gemm_split_noalloc_dev", "caps_autotune_entry",
+    "caps_leaf_gemm_split_noalloc_dev", "caps_autotune_entry", "caps_chol_mult_dev", "caps_chol_mult_host",
 ]
 
 
@@ -129,6 +129,11 @@ def lib() -> ctypes.CDLL:
         L.caps_release_cache.restype = None
         L.caps_leaf_gemm_split_noalloc_dev.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
         L.caps_leaf_gemm_split_noalloc_dev.restype = ctypes.c_int
+        i_, d_ = ctypes.c_int, ctypes.c_double
+        L.caps_chol_mult_dev.argtypes = [vp, vp, vp, i_, i_, i_, d_, ctypes.c_char_p, OP, vp]
+        L.caps_chol_mult_dev.restype = ctypes.c_int
+        L.caps_chol_mult_host.argtypes = [dp, dp, dp, i_, i_, i_, d_, ctypes.c_char_p, OP]
+        L.caps_chol_mult_host.restype = ctypes.c_int
         ip = ctypes.POINTER(ctypes.c_int)
         L.caps_autotune_entry.argtypes = [ctypes.c_int, ip, ip, ip, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
         L.caps_autotune_entry.restype = ctypes.c_int
@@ -213,6 +218,28 @@ def leaf_gemm(A, B, C, m: int, form: int | str = CAPS_FORM_PLAIN, slices: int = 
     opt = options(form, slices, diagonals, 0, scheme)
     _check(lib().caps_leaf_gemm_dev(_dev_ptr(A, "A"), _dev_ptr(B, "B"), _dev_ptr(C, "C"), int(m),
                                     ctypes.byref(opt), _stream_ptr(stream)))
+
+
+def chol_mult(C, A, B, n: int, r: int, alpha: float = 1.0, x: int = 1, pattern=None,
+              form: int | str = CAPS_FORM_PLAIN, slices: int = 0, diagonals: int = 0, stream=None,
+              scheme: int | str = 0) -> None:
+    """The Cholesky subproject's multiply (cholesky/mult.h:6, mult.cpp:11-28 on
+    one rank): C = alpha C - A B^T on n x n matrices in its recursive layout
+    with r levels (the CAPS layout with nrec = r, bs = 1).  The product runs
+    as this library's Strassen-Winograd multiply with r levels.  alpha = 0
+    leaves C unread.  Torch CUDA tensors run on `stream`; numpy arrays go
+    through the host entry point."""
+    opt = options(form, slices, diagonals, 0, scheme)
+    if isinstance(A, np.ndarray):
+        for t in (A, B, C):
+            if t.dtype != np.float64 or not t.flags.c_contiguous:
+                raise TypeError("host arrays must be contiguous float64")
+        dp = ctypes.POINTER(ctypes.c_double)
+        _check(lib().caps_chol_mult_host(C.ctypes.data_as(dp), A.ctypes.data_as(dp), B.ctypes.data_as(dp),
+                                         int(n), int(x), int(r), float(alpha), _pat(pattern), ctypes.byref(opt)))
+        return
+    _check(lib().caps_chol_mult_dev(_dev_ptr(C, "C"), _dev_ptr(A, "A"), _dev_ptr(B, "B"), int(n), int(x), int(r),
+                                    float(alpha), _pat(pattern), ctypes.byref(opt), _stream_ptr(stream)))
 
 
 NOALLOC_MAX_M = 512

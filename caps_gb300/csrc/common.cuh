@@ -81,6 +81,12 @@ cudaError_t launch_reorder(const double *const *src_dev, double *const *dst_dev,
                            int64_t n, int nrec, int64_t bs, bool to_caps, cudaStream_t stream);
 cudaError_t launch_reorder_one(const double *src, double *dst, int64_t n, int nrec, int64_t bs,
                                bool to_caps, cudaStream_t stream);
+// Transpose (times -1 when `negate`) of an n x n matrix in the recursive
+// layout with bs = 1; dst must not overlap src.
+cudaError_t launch_rec_transpose(const double *src, double *dst, int64_t n, int nrec, bool negate,
+                                 cudaStream_t stream);
+// c = alpha * c + p over `count` elements.
+cudaError_t launch_scale_add(double *c, const double *p, double alpha, int64_t count, cudaStream_t stream);
 
 // ---------------------------------------------------------------------------
 // Base-case GEMMs over a batch of leaves (column-major m x m each).

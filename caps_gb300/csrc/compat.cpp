@@ -276,3 +276,18 @@ void multiply(double *A, double *B, double *C, MatDescriptor desc, char *pattern
     cudaFree(dB);
     cudaFree(dC);
 }
+
+// --------------------------------------------------------------- cholesky/mult.cpp
+// The Cholesky subproject's multiply on one rank (cholesky/mult.cpp:11-28,
+// x = 1): C = alpha C - A B^T on host arrays in its recursive layout, the
+// product on the GPU.  The reference has no error return: a failure prints
+// and exits, as multiply() above does.
+void mult(double *C, double *A, double *B, int n, int x, int r, double alpha) {
+    caps_options opt;
+    caps_options_init(&opt);
+    opt.form = form_from_env();
+    opt.slices = g_slices;
+    caps_status st = caps_chol_mult_host(C, A, B, n, x, r, alpha, nullptr, &opt);
+    g_last_status = st;
+    if (st != CAPS_OK) die_status(st, "mult");
+}

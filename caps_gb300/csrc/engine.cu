@@ -85,6 +85,7 @@ static caps_status ensure(DevBuf &b, size_t bytes) {
 static DevBuf g_arena;   // workspace + task tables
 static DevBuf g_io;      // device copies for caps_multiply_host
 static DevBuf g_status;  // device status words of split kernels
+static DevBuf g_chol;    // -B^T and the product of caps_chol_mult_dev
 
 struct PinnedBuf {
     void *ptr = nullptr;
@@ -1185,6 +1186,58 @@ caps_status caps_leaf_gemm_dev(const double *A, const double *B, double *C, int 
     return caps_multiply_dev(A, B, C, d, "", opt, stream);
 }
 
+// The Cholesky subproject's update on one rank (cholesky/mult.cpp:11-28 with
+// x = 1): C = alpha C - A B^T.  -B^T is formed in the recursive layout (an
+// exact negation and transpose), A (-B^T) runs as this library's multiply
+// with r levels, and C = alpha C + product is one more pass; with alpha = 0
+// the multiply writes C directly and C is never read (dgemm's beta = 0 rule,
+// mult.cpp:91-98).
+static caps_status chol_mult_locked(double *C, const double *A, const double *B, int n, int x, int r,
+                                    double alpha, const char *pattern, const caps_options &o, cudaStream_t s) {
+    if (!A || !B || !C) return CAPS_ERR_ARG;
+    if (x != 1) {
+        g_last_err = "mult: x > 1 process groups need more than one rank";
+        return CAPS_ERR_UNSUPPORTED;
+    }
+    caps_desc d{n, r, 1, 1, 1, 1, 1};
+    CAPS_TRY(check_desc(d));
+    CAPS_TRY(check_pattern(d, pattern));
+    CAPS_TRY(check_opts(o));
+    const size_t nn = (size_t)n * n * sizeof(double), slot = (nn + 255) & ~(size_t)255;
+    const bool direct = alpha == 0.0;
+    CAPS_TRY(ensure(g_chol, direct ? slot : 2 * slot));
+    double *nbt = (double *)g_chol.ptr;
+    double *prod = direct ? C : (double *)(g_chol.ptr + slot);
+    CAPS_CUDA_TRY(launch_rec_transpose(B, nbt, n, r, true, s));
+    CAPS_TRY(multiply_dev_locked(A, nbt, prod, d, pattern, o, s, true));
+    if (!direct) CAPS_CUDA_TRY(launch_scale_add(C, prod, alpha, (int64_t)n * n, s));
+    return CAPS_OK;
+}
+
+caps_status caps_chol_mult_dev(double *C, const double *A, const double *B, int n, int x, int r, double alpha,
+                               const char *pattern, const caps_options *opt, void *stream) {
+    std::lock_guard<std::recursive_mutex> g(g_mu);
+    return chol_mult_locked(C, A, B, n, x, r, alpha, pattern, opts_or_default(opt), (cudaStream_t)stream);
+}
+
+caps_status caps_chol_mult_host(double *C, const double *A, const double *B, int n, int x, int r, double alpha,
+                                const char *pattern, const caps_options *opt) {
+    std::lock_guard<std::recursive_mutex> g(g_mu);
+    if (!A || !B || !C) return CAPS_ERR_ARG;
+    if (n <= 0) return CAPS_ERR_SIZE;
+    const size_t nn = (size_t)n * n * sizeof(double), slot = (nn + 255) & ~(size_t)255;
+    CAPS_TRY(ensure(g_io, 3 * slot));
+    double *dA = (double *)g_io.ptr, *dB = (double *)(g_io.ptr + slot), *dC = (double *)(g_io.ptr + 2 * slot);
+    cudaStream_t s = 0;
+    CAPS_CUDA_TRY(cudaMemcpyAsync(dA, A, nn, cudaMemcpyHostToDevice, s));
+    CAPS_CUDA_TRY(cudaMemcpyAsync(dB, B, nn, cudaMemcpyHostToDevice, s));
+    if (alpha != 0.0) CAPS_CUDA_TRY(cudaMemcpyAsync(dC, C, nn, cudaMemcpyHostToDevice, s));
+    CAPS_TRY(chol_mult_locked(dC, dA, dB, n, x, r, alpha, pattern, opts_or_default(opt), s));
+    CAPS_CUDA_TRY(cudaMemcpyAsync(C, dC, nn, cudaMemcpyDeviceToHost, s));
+    CAPS_CUDA_TRY(cudaStreamSynchronize(s));
+    return CAPS_OK;
+}
+
 caps_status caps_workspace_size(caps_desc desc, const char *pattern, const caps_options *opt, long long *bytes) {
     std::lock_guard<std::recursive_mutex> g(g_mu);
     CAPS_TRY(check_desc(desc));
@@ -1279,7 +1332,7 @@ void caps_release_cache(void) {
     cudaDeviceSynchronize();
     for (BatchPlan *p : g_batch_plans) free_plan(p);
     g_batch_plans.clear();
-    for (DevBuf *b : {&g_arena, &g_io, &g_status}) {
+    for (DevBuf *b : {&g_arena, &g_io, &g_status, &g_chol}) {
         if (b->ptr) cudaFree(b->ptr);
         *b = DevBuf();
     }

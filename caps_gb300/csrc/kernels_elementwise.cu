@@ -396,4 +396,86 @@ cudaError_t launch_reorder_one(const double *src, double *dst, int64_t n, int nr
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Transpose in the recursive layout with bs = 1 (leaves column-major m x m),
+// times `sign` (+1 or -1, exact).  X^T has quadrants 11 = X11^T, 21 = X12^T,
+// 12 = X21^T, 22 = X22^T at every level, so leaf L of X^T is the transpose
+// of the leaf whose base-4 digits are L's with the row and column bit of
+// each digit swapped.  One block moves one 32 x 32 tile through shared
+// memory, reads and writes both coalesced; grid-stride over (leaf, tile).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) rec_transpose_kernel(const double *__restrict__ s, double *__restrict__ d,
+                                                            int64_t m, int64_t leaves, int64_t tside, double sign) {
+    __shared__ double tile[32][33];
+    const int64_t per_leaf = tside * tside, total = leaves * per_leaf, mm = m * m;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int64_t it = blockIdx.x; it < total; it += gridDim.x) {
+        const int64_t leaf = it / per_leaf, t = it - leaf * per_leaf;
+        const int64_t ti = t % tside, tj = t / tside;  // destination tile (row, column)
+        const uint64_t L = (uint64_t)leaf;
+        const int64_t sleaf = (int64_t)(((L & 0x5555555555555555ull) << 1) | ((L >> 1) & 0x5555555555555555ull));
+        const double *sl = s + sleaf * mm;
+        double *dl = d + leaf * mm;
+        // destination (i, j) = source (j, i): tile (ti, tj) reads source rows
+        // tj*32.., columns ti*32..; tile[c][r] holds source (tj*32 + r, ti*32 + c)
+        for (int k = ty; k < 32; k += 8) {
+            const int64_t r = tj * 32 + tx, c = ti * 32 + k;
+            if (r < m && c < m) tile[k][tx] = sl[r + c * m];
+        }
+        __syncthreads();
+        for (int k = ty; k < 32; k += 8) {
+            const int64_t i = ti * 32 + tx, j = tj * 32 + k;
+            if (i < m && j < m) dl[i + j * m] = sign * tile[tx][k];
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_rec_transpose(const double *src, double *dst, int64_t n, int nrec, bool negate,
+                                 cudaStream_t stream) {
+    const int64_t m = n >> nrec, leaves = (int64_t)1 << (2 * nrec), tside = (m + 31) / 32;
+    const int64_t total = leaves * tside * tside;
+    const int64_t blocks = total < 152 * 16 ? total : 152 * 16;
+    rec_transpose_kernel<<<(unsigned)blocks, 256, 0, stream>>>(src, dst, m, leaves, tside, negate ? -1.0 : 1.0);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// C = alpha * C + P, the product rounded, then the sum (the order of a dgemm
+// that scales C by beta before accumulating); alpha = 1 makes the first step
+// exact.  16-byte aligned pointers take two elements per load.
+template <bool VEC>
+__global__ void __launch_bounds__(256) scale_add_kernel(double *__restrict__ c, const double *__restrict__ p,
+                                                        double alpha, int64_t count) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    if (VEC) {
+        double2 *c2 = reinterpret_cast<double2 *>(c);
+        const double2 *p2 = reinterpret_cast<const double2 *>(p);
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count / 2; i += stride) {
+            double2 x = c2[i];
+            const double2 y = __ldcs(p2 + i);
+            x.x = __dadd_rn(__dmul_rn(alpha, x.x), y.x);
+            x.y = __dadd_rn(__dmul_rn(alpha, x.y), y.y);
+            c2[i] = x;
+        }
+    } else {
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride)
+            c[i] = __dadd_rn(__dmul_rn(alpha, c[i]), __ldcs(p + i));
+    }
+}
+
+cudaError_t launch_scale_add(double *c, const double *p, double alpha, int64_t count, cudaStream_t stream) {
+    if (count <= 0) return cudaSuccess;
+    const bool vec = (((uintptr_t)c | (uintptr_t)p) & 15) == 0 && count % 2 == 0;
+    const int64_t work = vec ? count / 2 : count;
+    int64_t blocks = (work + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (vec)
+        scale_add_kernel<true><<<(unsigned)blocks, 256, 0, stream>>>(c, p, alpha, count);
+    else
+        scale_add_kernel<false><<<(unsigned)blocks, 256, 0, stream>>>(c, p, alpha, count);
+    count_launch();
+    return cudaGetLastError();
+}
+
 }  // namespace caps

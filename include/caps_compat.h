@@ -17,6 +17,7 @@
  *   initTimers, startTimer, stopTimer, printCounters, increase*
  *                       counters.h:5-21
  *   read_timer          library.h:8          SEVEN library.h:5
+ *   mult                cholesky/mult.h:6   (cholesky/mult.cpp:11-28, one rank)
  *
  * Differences, all forced by one GPU per process:
  *   - one rank: getRank() = 0, getLog7nProcs() = 0, getPFactor() = 1;
@@ -45,6 +46,10 @@ const int DESC_SIZE = 7;
 const int SEVEN = 7;
 
 void multiply(double *A, double *B, double *C, MatDescriptor desc, char *pattern = 0);
+
+/* The Cholesky subproject's multiply (cholesky/mult.h:6): C = alpha C - A B^T
+ * on n x n host arrays in its recursive layout, one rank (x = 1). */
+void mult(double *C, double *A, double *B, int n, int x, int r, double alpha = 1.);
 
 void verifyDescriptor(MatDescriptor desc);
 long long numEntriesPerProc(MatDescriptor desc);

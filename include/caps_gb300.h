@@ -125,6 +125,26 @@ caps_status caps_leaf_gemm_dev(const double *A, const double *B, double *C, int 
 caps_status caps_leaf_gemm_split_noalloc_dev(const double *A, const double *B, double *C, int m,
                                              int slices, int diagonals, void *stream);
 
+/* The Cholesky subproject's multiply, C = alpha * C - A * B^T, on one rank
+ * (cholesky/mult.h:6, `mult(C, A, B, n, x, r, alpha)`, mult.cpp:11-28 with
+ * x = 1: multBase :76-107 below 1024 or at r = 0, multDFS :109-137 above).
+ * n x n matrices in that subproject's recursive layout (cholesky/pack.cpp:
+ * 2-49: r levels of quadrants 11, 21, 12, 22, then column-major blocks of
+ * n / 2^r) -- the CAPS layout with nrec = r and bs = 1.  The product runs as
+ * this library's Strassen-Winograd multiply with r levels (pattern and opt
+ * as for caps_multiply_dev); the reference's is classical, so float results
+ * differ within the Strassen error bound, and integer-valued data give the
+ * same bits.  alpha = 0 leaves C unread (dgemm's beta = 0).  x must be 1
+ * (CAPS_ERR_UNSUPPORTED otherwise); n % 2^r != 0 gives CAPS_ERR_SIZE.  C must
+ * not overlap A or B.  Device pointers, asynchronous on `stream` apart from
+ * the split form's status read. */
+caps_status caps_chol_mult_dev(double *C, const double *A, const double *B, int n, int x, int r,
+                               double alpha, const char *pattern, const caps_options *opt, void *stream);
+
+/* Same on host arrays: copies in, updates, copies C back, synchronises. */
+caps_status caps_chol_mult_host(double *C, const double *A, const double *B, int n, int x, int r,
+                                double alpha, const char *pattern, const caps_options *opt);
+
 /* Workspace bytes caps_multiply_dev needs for (desc, pattern, opt). */
 caps_status caps_workspace_size(caps_desc desc, const char *pattern, const caps_options *opt,
                                 long long *bytes);

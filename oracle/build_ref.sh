@@ -4,6 +4,7 @@
 # reference sources are present; outputs never leave oracle/_ref/ (git-ignored).
 #   oracle/_ref/fromfile1, oracle/_ref/randombenchmark   the reference drivers
 #   oracle/_ref/libcapsref.so                           multiply() & friends
+#   oracle/_ref/libcholref.so                           cholesky/ mult() & friends
 # Usage: oracle/build_ref.sh [REFERENCE_DIR] [THREADS]
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
@@ -26,5 +27,13 @@ link="$out/blas_lp64.o $blaslib -Wl,-rpath,$blasdir"
 $CXX -shared -o "$out/libcapsref.so" $objs $link
 $CXX "$ref/fromfile1.cpp" $objs $link -o "$out/fromfile1"
 $CXX "$ref/randombenchmark.cpp" $objs $link -o "$out/randombenchmark"
+# the Cholesky subproject's multiply, mult() (cholesky/mult.cpp), one rank
+chol="$ref/cholesky"
+cobjs=""
+for s in mult.cpp sizes.cpp communication.cpp counters.cpp library.cpp; do
+  $CXX -fPIC -I"$chol" -c "$chol/$s" -o "$out/chol_${s%.cpp}.o"
+  cobjs="$cobjs $out/chol_${s%.cpp}.o"
+done
+$CXX -shared -o "$out/libcholref.so" $cobjs $link
 rm -f "$out"/*.o
 echo "built $out (threads=$threads, blas=$blaslib)"

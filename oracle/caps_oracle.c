@@ -20,6 +20,8 @@
  *   - base case with bs repack:                 multiply.cpp:1082-1141,
  *                                               dgemm-blas.cpp:4-13
  *   - pattern dispatch on one rank:             multiply.cpp:28-108
+ *   - the Cholesky subproject's multiply,       cholesky/mult.cpp:11-137,
+ *     C = alpha C - A B^T, on one rank:         cholesky/pack.cpp:2-49
  * plus a double-double classical product (Ogita, Rump, Oishi 2005, "Accurate
  * sum and dot product", algorithm Dot2) used as the float oracle, and a CPU
  * model of the split-integer base case that the GPU form must match exactly.
@@ -292,6 +294,82 @@ int caps_oracle_multiply_sample(const double *A, const double *B, double *C, int
 /* add/multiply counters as the reference counts them (counters.cpp). */
 void caps_oracle_counters(int64_t *adds, int64_t *muls) { *adds = g_adds; *muls = g_muls; }
 void caps_oracle_reset_counters(void) { g_adds = 0; g_muls = 0; }
+
+/* ---------------------------------------------------------------------- */
+/* The Cholesky subproject's multiply on one rank: C = alpha C - A B^T.    */
+/* cholesky/mult.cpp:11-28 (dispatch, x = 1), multBase :76-107, multDFS    */
+/* :109-137, pack / unpack cholesky/pack.cpp:2-49.  Its recursive layout   */
+/* is the CAPS layout above with nrec = r, bs = 1.  At r = 0 or n <= 1024  */
+/* (the reference's minsize) the block is unpacked to column-major and     */
+/* updated by one dgemm('N', 'T', alpha = -1, beta = alpha); above, the    */
+/* eight quadrant updates run in the reference's order, the first of each  */
+/* pair with alpha and the second with 1.  alpha = 0 leaves C unread.      */
+/* ---------------------------------------------------------------------- */
+static const int64_t CHOL_MINSIZE = 1024;   /* mult.cpp:9 */
+
+static void chol_base(int64_t n, int r, double alpha, double *C, const double *A, const double *B)
+{
+    int64_t nn = n * n;
+    double *w = r ? (double *)malloc((size_t)(3 * nn) * sizeof(double)) : 0;
+    const double *AA = A, *BB = B;
+    double *CC = C;
+    if (r) {
+        double *a = w, *b = w + nn;
+        CC = w + 2 * nn;
+        caps_oracle_from_caps(n, r, 1, A, a);
+        caps_oracle_from_caps(n, r, 1, B, b);
+        if (alpha != 0.0) caps_oracle_from_caps(n, r, 1, C, CC);
+        AA = a;
+        BB = b;
+    }
+    if (g_dgemm) {
+        const char N = 'N', T = 'T';
+        const double none = -1.0;
+        g_dgemm(&N, &T, &n, &n, &n, &none, AA, &n, BB, &n, &alpha, CC, &n);
+    } else {
+        /* rows of A and of B made contiguous, k ascending in each sum */
+        double *at = (double *)malloc((size_t)(2 * nn) * sizeof(double)), *bt = at + nn;
+        for (int64_t k = 0; k < n; k++)
+            for (int64_t i = 0; i < n; i++) {
+                at[i * n + k] = AA[i + k * n];
+                bt[i * n + k] = BB[i + k * n];
+            }
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+        for (int64_t j = 0; j < n; j++)
+            for (int64_t i = 0; i < n; i++) {
+                double acc = 0.0;
+                const double *a = at + i * n, *b = bt + j * n;
+                for (int64_t k = 0; k < n; k++) acc += a[k] * b[k];
+                double c = alpha == 0.0 ? 0.0 : alpha * CC[i + j * n];
+                CC[i + j * n] = c - acc;
+            }
+        free(at);
+    }
+    if (r) {
+        caps_oracle_to_caps(n, r, 1, CC, C);
+        free(w);
+    }
+}
+
+void caps_oracle_chol_mult(double *C, const double *A, const double *B, int64_t n, int r, double alpha)
+{
+    if (r == 0 || n <= CHOL_MINSIZE) {
+        chol_base(n, r, alpha, C, A, B);
+        return;
+    }
+    int64_t h = n / 2, q = h * h;
+    double *C11 = C, *C21 = C + q, *C12 = C + 2 * q, *C22 = C + 3 * q;
+    const double *A11 = A, *A21 = A + q, *A12 = A + 2 * q, *A22 = A + 3 * q;
+    const double *B11 = B, *B21 = B + q, *B12 = B + 2 * q, *B22 = B + 3 * q;
+    caps_oracle_chol_mult(C11, A11, B11, h, r - 1, alpha);
+    caps_oracle_chol_mult(C11, A12, B12, h, r - 1, 1.0);
+    caps_oracle_chol_mult(C12, A11, B21, h, r - 1, alpha);
+    caps_oracle_chol_mult(C12, A12, B22, h, r - 1, 1.0);
+    caps_oracle_chol_mult(C21, A21, B11, h, r - 1, alpha);
+    caps_oracle_chol_mult(C21, A22, B12, h, r - 1, 1.0);
+    caps_oracle_chol_mult(C22, A21, B21, h, r - 1, alpha);
+    caps_oracle_chol_mult(C22, A22, B22, h, r - 1, 1.0);
+}
 
 /* ---------------------------------------------------------------------- */
 /* Double-double classical product (Dot2 of Ogita-Rump-Oishi):             */

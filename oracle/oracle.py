@@ -85,6 +85,8 @@ def lib():
         L.caps_oracle_multiply_sample.restype = ctypes.c_int
         L.caps_oracle_multiply_sample.argtypes = [_dp, _dp, _dp, ctypes.c_int64, ctypes.c_int, ctypes.c_int64,
                                                   ctypes.c_char_p, ctypes.c_int, _dp, _dp]
+        L.caps_oracle_chol_mult.restype = None
+        L.caps_oracle_chol_mult.argtypes = [_dp, _dp, _dp, ctypes.c_int64, ctypes.c_int, ctypes.c_double]
         L.caps_oracle_set_threads(os.cpu_count() or 1)
         _lib = L
     return _lib
@@ -151,6 +153,17 @@ def multiply(A: np.ndarray, B: np.ndarray, n: int, nrec: int, bs: int = 1,
     if rc == -2:
         raise ValueError("matrix size not divisible by 2^nrec*bs")
     return C
+
+
+def chol_mult(C: np.ndarray, A: np.ndarray, B: np.ndarray, n: int, r: int, alpha: float = 1.0) -> np.ndarray:
+    """The Cholesky subproject's multiply on one rank (cholesky/mult.cpp:11-137):
+    alpha C - A B^T for flat float64 matrices in its recursive layout (the CAPS
+    layout with nrec = r, bs = 1).  Returns a new array; C is unread when
+    alpha = 0."""
+    out = np.array(C, dtype=np.float64, copy=True) if alpha != 0 else np.empty(n * n, dtype=np.float64)
+    lib().caps_oracle_chol_mult(_p(out), _p(np.ascontiguousarray(A, dtype=np.float64)),
+                                _p(np.ascontiguousarray(B, dtype=np.float64)), n, r, float(alpha))
+    return out
 
 
 def multiply_sample(A: np.ndarray, B: np.ndarray, C: np.ndarray, n: int, nrec: int, bs: int = 1,

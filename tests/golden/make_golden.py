@@ -14,6 +14,9 @@ one-rank build (oracle/build_ref.sh -> oracle/_ref/libcapsref.so) exist:
    layout; the oracle with the same BLAS must reproduce them bit for bit.
 3. ref_layout.npz -- the reference's distributeFrom1Proc applied to the ramp
    0..n^2-1 (column-major), i.e. the CAPS layout permutation.
+4. ref_chol.npz -- outputs of the Cholesky subproject's own mult()
+   (cholesky/mult.cpp, one rank; oracle/_ref/libcholref.so) on seeded
+   inputs in its recursive layout: C = alpha C - A B^T.
 """
 import ctypes
 import hashlib
@@ -102,9 +105,51 @@ def ref_layout(reflib):
     print("ref_layout.npz:", list(out))
 
 
+# The Cholesky subproject's mult() (C = alpha C - A B^T, cholesky/mult.cpp),
+# one rank: (n, r, alpha, kind, seed).  n = 2048 > 1024 runs its DFS branch;
+# that output is stored as a SHA-256 (the test regenerates the inputs).
+CHOL_CASES = [(32, 0, 1.0, "float", 21), (64, 2, 1.0, "float", 22), (96, 1, 0.0, "float", 23),
+              (128, 3, 2.5, "float", 24), (56, 2, 1.0, "int", 25), (2048, 2, 1.0, "float", 26),
+              (2048, 1, 0.5, "int", 27)]
+
+
+def chol_inputs(n, kind, seed):
+    rng = np.random.default_rng(seed)
+    if kind == "int":
+        return [rng.integers(-9, 10, n * n).astype(np.float64) for _ in range(3)]
+    return [rng.uniform(-1, 1, n * n) for _ in range(3)]
+
+
+def ref_chol(chollib):
+    L = ctypes.CDLL(chollib)
+    argc = ctypes.c_int(0)
+    argv = ctypes.POINTER(ctypes.c_char_p)()
+    getattr(L, "_Z17initCommunicationPiPPPc")(ctypes.byref(argc), ctypes.byref(argv))
+    getattr(L, "_Z10initTimersv")()
+    init_sizes = getattr(L, "_Z9initSizesiii")
+    init_sizes.argtypes = [ctypes.c_int] * 3
+    mult = getattr(L, "_Z4multPdS_S_iiid")
+    dp = ctypes.POINTER(ctypes.c_double)
+    mult.argtypes = [dp, dp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+    mult.restype = None
+    out = {}
+    for n, r, alpha, kind, seed in CHOL_CASES:
+        A, B, C = chol_inputs(n, kind, seed)
+        init_sizes(1, r, n)
+        mult(C.ctypes.data_as(dp), A.ctypes.data_as(dp), B.ctypes.data_as(dp), n, 1, r, alpha)
+        key = "chol_%d_%d_%s" % (n, r, kind)
+        if n > 256:
+            out[key + "_sha256"] = np.frombuffer(hashlib.sha256(C.tobytes()).digest(), dtype=np.uint8)
+        else:
+            out[key] = C
+    np.savez_compressed(os.path.join(HERE, "ref_chol.npz"), **out)
+    print("ref_chol.npz:", list(out))
+
+
 if __name__ == "__main__":
     refdir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     reflib = os.path.join(ROOT, "oracle", "_ref", "libcapsref.so")
     ref_tests(refdir)
     ref_float(reflib)
     ref_layout(reflib)
+    ref_chol(os.path.join(ROOT, "oracle", "_ref", "libcholref.so"))

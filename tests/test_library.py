@@ -1,6 +1,7 @@
 """CPU tests of the product library: it loads, exports every declared symbol,
 and its host-side logic (validation, pattern choice, workspace sizing, error
 codes) behaves like the reference's entry points.  No kernel runs here."""
+import ctypes
 import os
 import re
 import subprocess
@@ -121,3 +122,18 @@ def test_hybrid_factor_outside_reference_range_rejected(caps):
         with pytest.raises(caps.CapsError) as e:
             caps.workspace_size(caps.MatDescriptor.make(1024, 2, 1, k), "hh")
         assert e.value.status == 7  # CAPS_ERR_UNSUPPORTED
+
+
+def test_chol_mult_validation_before_any_device_work(caps):
+    """The Cholesky mult() entry point rejects bad arguments before it touches
+    the device: x > 1 (more than one rank), n not divisible by 2^r, a bad
+    pattern char, NULL pointers."""
+    L = caps.lib()
+    p = ctypes.c_void_p(4096)  # never dereferenced: every call below fails its checks first
+    opt = caps.options("plain")
+    call = lambda C, A, B, n, x, r, pat=None: L.caps_chol_mult_dev(C, A, B, n, x, r, 1.0, pat, ctypes.byref(opt), None)
+    assert call(p, p, p, 64, 2, 1) == 7
+    assert call(p, p, p, 54, 1, 2) == 2
+    assert call(p, p, p, 0, 1, 0) == 2
+    assert call(p, p, p, 64, 1, 2, b"dx") == 1
+    assert call(None, p, p, 64, 1, 2) == 8

@@ -230,3 +230,55 @@ def test_residue_model_matches_exact_rounding(oracle_mod, kind):
     Cp, tp = _residue_model_py(A, B)
     assert t == tp
     assert np.array_equal(C.reshape(m, m).T, Cp)
+
+
+def _golden_module():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mg", os.path.join(ROOT, "tests", "golden", "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    return mg
+
+
+def test_chol_mult_oracle_matches_reference_mult(oracle_mod):
+    """The restated Cholesky mult() (C = alpha C - A B^T, one rank) with numpy's
+    OpenBLAS reproduces the subproject's own mult() bit for bit, its DFS branch
+    (n = 2048 > 1024) included."""
+    if not oracle_mod.use_blas(True):
+        pytest.skip("numpy OpenBLAS not found")
+    mg = _golden_module()
+    g = np.load(os.path.join(ROOT, "tests", "golden", "ref_chol.npz"))
+    try:
+        for n, r, alpha, kind, seed in mg.CHOL_CASES:
+            A, B, C = mg.chol_inputs(n, kind, seed)
+            out = oracle_mod.chol_mult(C, A, B, n, r, alpha)
+            key = "chol_%d_%d_%s" % (n, r, kind)
+            if key in g.files:
+                assert np.array_equal(out, g[key]), key
+            else:
+                assert hashlib.sha256(out.tobytes()).digest() == bytes(g[key + "_sha256"]), key
+    finally:
+        oracle_mod.use_blas(False)
+
+
+@pytest.mark.parametrize("n,r,alpha", [(56, 2, 1.0), (64, 3, 0.0), (2048, 1, -3.0)])
+def test_chol_mult_oracle_integers_exact(oracle_mod, n, r, alpha):
+    """Integer data: the oracle equals the exact alpha C - A B^T, with or
+    without a BLAS; alpha = 0 leaves C unread (C holds NaN here)."""
+    rng = np.random.default_rng(n + r)
+    A, B, C = (rng.integers(-9, 10, n * n).astype(np.float64) for _ in range(3))
+    if alpha == 0:
+        C[:] = np.nan
+    # |entries| <= 9: every partial sum of the float64 product is an integer
+    # below 2^53, so numpy's float product is exact
+    Af, Bf = mat_of(oracle_mod, A, n, r, 1), mat_of(oracle_mod, B, n, r, 1)
+    Cf = np.zeros((n, n)) if alpha == 0 else mat_of(oracle_mod, C, n, r, 1)
+    exact = alpha * Cf - Af @ Bf.T
+    for blas in (False, True):
+        if blas and not oracle_mod.use_blas(True):
+            continue
+        try:
+            out = oracle_mod.chol_mult(C, A, B, n, r, alpha)
+        finally:
+            oracle_mod.use_blas(False)
+        assert np.array_equal(mat_of(oracle_mod, out, n, r, 1), exact), (n, r, alpha, blas)
