@@ -58,10 +58,11 @@ def parse():
     ap.add_argument("--no-wide", action="store_true", help="skip the wide-range (u*2^k) error check")
     ap.add_argument("--samples", type=int, default=256, help="entries checked against binary128")
     ap.add_argument("--workload", default="split16384",
-                    choices=["split16384", "plain8192", "batched512", "int32768"],
+                    choices=["split16384", "plain8192", "batched512", "int32768", "chol16384"],
                     help="split16384: the headline (n=16384, r=3, split vs FP64); plain8192: FP64 Strassen "
                          "n=8192 r=3 'ddd'; batched512: 512 uneven multiplies; int32768: n=32768 r=4 'bbdd' "
-                         "integers under a 120 GB budget")
+                         "integers under a 120 GB budget; chol16384: the Cholesky subproject's update "
+                         "C = C - A B^T, n=16384, r=3")
     return ap.parse_args()
 
 
@@ -427,6 +428,143 @@ def run_int32768(args, world, rank, local):
                                      split_vs_plain=res["split"]["value"] / res["plain"]["value"])), flush=True)
 
 
+def chol_sampled_error(out_cm, C0_cm, A_cm, B_cm, n, samples, seed=7):
+    """C = C0 - A B^T on sampled entries: max |C - C_ref| / (|C0| + |A||B^T|)
+    and normwise; C_ref in binary128 (numpy longdouble)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    ld = np.longdouble
+    Am, Bm = A_cm.reshape(n, n), B_cm.reshape(n, n)  # [col][row]
+    Om, Cm = out_cm.reshape(n, n), C0_cm.reshape(n, n)
+    ew, num, den = 0.0, 0.0, 0.0
+    for i, j in zip(rng.integers(0, n, samples), rng.integers(0, n, samples)):
+        a, b = np.ascontiguousarray(Am[:, i]), np.ascontiguousarray(Bm[:, j])  # rows i of A, j of B
+        ref = ld(Cm[j, i]) - np.dot(a.astype(ld), b.astype(ld))
+        scale = abs(float(Cm[j, i])) + float(np.dot(np.abs(a), np.abs(b)))
+        d = float(ld(Om[j, i]) - ref)
+        ew = max(ew, abs(d) / scale if scale > 0 else abs(d))
+        num += d * d
+        den += float(ref) ** 2
+    return {"max_elementwise_rel": ew, "normwise_rel": (num / den) ** 0.5 if den > 0 else 0.0,
+            "samples": int(samples)}
+
+
+def run_chol16384(args, world, rank, local):
+    """The Cholesky subproject's trailing update C = C - A B^T (cholesky/mult.h:6,
+    mult.cpp:11-137 on one rank) at n=16384 in its recursive layout with r=3,
+    uniform[-1,1) inputs: -B^T formed on the device, the product by the split
+    Strassen multiply, one scale-add pass."""
+    import numpy as np
+    import torch
+    import caps_gb300 as cg
+    dev = torch.device("cuda", local)
+    n, r = 16384, 3
+    desc = cg.MatDescriptor.make(n, r)
+    g = torch.Generator(device=dev)
+    g.manual_seed(31 + rank)
+    A, B, C0 = (torch.rand(n * n, dtype=torch.float64, device=dev, generator=g) * 2 - 1 for _ in range(3))
+    C = C0.clone()
+    stream = torch.cuda.current_stream(dev)
+    hA, hB, hC = (torch.empty(n * n, dtype=torch.float64, pin_memory=True) for _ in range(3))
+    hA.copy_(A)
+    hB.copy_(B)
+    hC.copy_(C0)
+
+    def step():
+        cg.chol_mult(C, A, B, n, r, 1.0, form="split", stream=stream.cuda_stream, scheme=args.scheme)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    cg.set_phase_timing(True)
+    gemm_t, gemm_launches, gemm_m3, launches = 0.0, 0, 0.0, 0
+    barrier(world)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+            c = cg.counters()
+            gemm_t += c["time_leaf_gemm"]
+            gemm_launches += c["leaf_gemm_launches"]
+            gemm_m3 += c["leaf_gemm_m3"]
+            launches += c["kernel_launches"] + 2  # the transpose and the scale-add
+        e1.record(stream)
+        torch.cuda.synchronize()
+    cg.set_phase_timing(False)
+    t = max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps, world)
+    moduli = cg.counters()["split_moduli"]
+    pattern = cg.resolve_pattern(desc, None, form="split")
+
+    # e2e: the host entry point with pinned host buffers (A, B, C in; C out)
+    nA, nB, nC = hA.numpy(), hB.numpy(), hC.numpy()
+    cg.chol_mult(nC, nA, nB, n, r, 1.0, form="split", scheme=args.scheme)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cg.chol_mult(nC, nA, nB, n, r, 1.0, form="split", scheme=args.scheme)
+    t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
+    if rank != 0:
+        return
+    # accuracy of one update from the seeded C0
+    C.copy_(C0)
+    step()
+    torch.cuda.synchronize()
+
+    def colmajor(x):
+        y = torch.empty_like(x)
+        cg.from_caps_layout(x, y, desc)
+        torch.cuda.synchronize()
+        return y.cpu().numpy()
+    err = chol_sampled_error(colmajor(C), colmajor(C0), colmajor(A), colmajor(B), n, args.samples)
+    peaks, peak_src = measured_peaks()
+    per_launch_flops = 2.0 * moduli * gemm_m3 / max(gemm_launches, 1)
+    per_launch_s = gemm_t / max(gemm_launches, 1)
+    achieved = per_launch_flops / per_launch_s / 1e12 if per_launch_s > 0 else 0.0
+    peak = float(peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops", 1700.0)))
+    cpu = None
+    if not args.no_cpu:
+        # the reference's path at n=16384, r=3 is multDFS down to 512 base
+        # updates of 2048 (r = 0: no repack), each one dgemm('N','T')
+        from oracle import oracle
+        cores = os.cpu_count() or 1
+        oracle.build()
+        blas = oracle.use_blas(True, threads=cores)
+        oracle.set_threads(cores)
+        rng = np.random.default_rng(12)
+        m = 2048
+        a, b, c0 = (rng.uniform(-1, 1, m * m) for _ in range(3))
+        oracle.chol_mult(c0, a, b, m, 0, 1.0)
+        reps = 3
+        tb0 = time.perf_counter()
+        for _ in range(reps):
+            oracle.chol_mult(c0, a, b, m, 0, 1.0)
+        t_base = (time.perf_counter() - tb0) / reps
+        cpu = {"value": 2.0 * n ** 3 / (512 * t_base) / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+               "sample": "oracle restatement of cholesky mult() (one rank, %s dgemm, %d threads): one base "
+                         "update of 2048 (r = 0) timed %d times (%.3f s each); the n=16384 r=3 update is "
+                         "512 of them (multDFS), value = 2n^3 / (512 t_base)" % (
+                             "OpenBLAS" if blas else "loop", cores, reps, t_base)}
+    print(json.dumps(common_line(
+        "effective TFLOP/s (2n³/t), Cholesky update C = C - A B^T, n=16384 r=3", world * 2.0 * n ** 3 / t / 1e12,
+        args, world, t * 1e3,
+        {"workload": "cholesky mult() C = C - A B^T, n=16384, r=3 recursive layout, split form "
+                     "(residues modulo %d moduli)" % moduli, "n": n, "nrec": r, "pattern": pattern,
+         "form": "split", "alpha": 1.0, "inputs": "float64 uniform[-1,1) seeded (torch.Generator)",
+         "l2": "inputs larger than L2 (each matrix 2 GiB vs 129 MB L2)"},
+        error=err,
+        roofline={"bound": "tensor", "kernel": "crt_gemm_kernel" if moduli else "split_gemm_kernel",
+                  "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                  "traffic": profiled_traffic("crt_gemm_kernel" if moduli else "split_gemm_kernel"),
+                  "peak_source": "%s bf16_tflops_sustained" % peak_src, "launches": gemm_launches,
+                  "avg_launch_ms": per_launch_s * 1e3},
+        cpu_baseline=cpu,
+        e2e={"value": world * 2.0 * n ** 3 / t_e2e / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": 3 * n * n * 8,
+             "d2h_bytes_per_step": n * n * 8, "ms_per_step": t_e2e * 1e3,
+             "api": "caps_chol_mult_host, pinned host buffers"},
+        gpu_launches=launches, clocks=clk.summary())), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup(args)
@@ -439,7 +577,8 @@ def main():
         from caps_gb300 import build as cbuild
         if not os.path.exists(cbuild.LIB):
             cbuild.build()
-        {"plain8192": run_plain8192, "batched512": run_batched512, "int32768": run_int32768}[args.workload](
+        {"plain8192": run_plain8192, "batched512": run_batched512, "int32768": run_int32768,
+         "chol16384": run_chol16384}[args.workload](
             args, world, rank, local)
         if world > 1:
             import torch.distributed as dist
