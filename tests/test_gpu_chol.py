@@ -10,7 +10,7 @@ import os
 import numpy as np
 import pytest
 
-from helpers import mat_of, dd_of
+from helpers import caps_of, mat_of, dd_of
 
 pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -79,21 +79,30 @@ def test_chol_mult_reference_integer_goldens(caps, oracle_mod, cuda):
 
 @pytest.mark.parametrize("form", ["plain", "split"])
 def test_chol_mult_float_error_vs_reference(caps, oracle_mod, cuda, form):
-    """Float data: the reference's classical update is pinned only by its
-    own outputs, so the GPU result is held to the reference's error (both
-    against a double-double product): at most 8x the reference's scaled
-    error plus 2^-52 (Strassen's r levels against a classical sum)."""
+    """Float data.  The reference's classical update is pinned only by its own
+    outputs (ref_chol.npz); this library's product is Strassen-Winograd with r
+    levels, whose error grows with r (9x the classical error at n = 128, r = 3
+    for FP64 leaves).  So the GPU result is held to the oracle's restatement
+    of the same Strassen update -- alpha C + A (-B^T) with r 'd' steps and
+    classical leaves, then one scale-add -- at most 2x its scaled error plus
+    2^-52, and to 2^-40 outright; both errors against a double-double
+    product, scaled by |alpha C| + |A| |B|^T."""
     mg = golden_module()
     g = np.load(os.path.join(ROOT, "tests", "golden", "ref_chol.npz"))
+    oracle_mod.use_blas(False)
     for n, r, alpha, kind, seed in mg.CHOL_CASES:
         key = "chol_%d_%d_%s" % (n, r, kind)
         if kind != "float" or key not in g.files:
             continue
         A, B, C = mg.chol_inputs(n, kind, seed)
         out = gpu_chol(caps, A, B, C, n, r, alpha, form=form)
-        e_ref = scaled_error(oracle_mod, g[key], A, B, C, n, r, alpha)
+        nbt = caps_of(oracle_mod, -np.ascontiguousarray(mat_of(oracle_mod, B, n, r, 1).T), r)
+        prod = oracle_mod.multiply(A, nbt, n, r, 1, "d" * r)
+        strassen = prod if alpha == 0 else alpha * C + prod
+        e_str = scaled_error(oracle_mod, strassen, A, B, C, n, r, alpha)
         e_gpu = scaled_error(oracle_mod, out, A, B, C, n, r, alpha)
-        assert e_gpu <= 8 * e_ref + 2.0 ** -52, (key, form, e_gpu, e_ref)
+        e_ref = scaled_error(oracle_mod, g[key], A, B, C, n, r, alpha)
+        assert e_gpu <= 2 * e_str + 2.0 ** -52 and e_gpu <= 2.0 ** -40, (key, form, e_gpu, e_str, e_ref)
 
 
 def test_chol_mult_host_entry_and_cxx_mult(caps, oracle_mod, cuda):
