@@ -61,61 +61,103 @@ size_t split_workspace_bytes(int m, int count, int scheme) {
 }
 
 // ---------------------------------------------------------------- scan
-// grid.y = 0: A rows, a thread per row and a block per (256 rows, 256-column
-// slab); grid.y = 1: B columns, a warp per column.
+// Per row of A and per column of B: the largest exponent and the lowest set
+// bit over the leaf.  Work units of up to 64K elements each, the same on both
+// sides: grid.y = 0, a block of A rows (512, a thread per two adjacent rows)
+// times a slab of 128 columns; grid.y = 1, a block of 32 B columns (a warp
+// per 4 columns).  16-byte loads when the leaf's element pairs are 16-byte
+// aligned (m even, base aligned), 8-byte loads otherwise.  grid.x strides
+// over (leaf, unit).
+constexpr int SCAN_AROWS = 512, SCAN_KSLAB = 128, SCAN_BCOLS = 32;
+
+__device__ __forceinline__ void scan_value(double x, int &emax, int &lmin) {
+    if ((unsigned long long)__double_as_longlong(x) << 1) {  // x != 0 by its encoding (an FP64 compare runs at 1/64 rate)
+        int E, lb;
+        exp_lsb(x, E, lb);
+        emax = E > emax ? E : emax;
+        lmin = lb < lmin ? lb : lmin;
+    }
+}
+
+__device__ __forceinline__ int64_t scan_units(int64_t M) {
+    const int64_t a = ((M + SCAN_AROWS - 1) / SCAN_AROWS) * ((M + SCAN_KSLAB - 1) / SCAN_KSLAB);
+    const int64_t b = (M + SCAN_BCOLS - 1) / SCAN_BCOLS;
+    return a > b ? a : b;
+}
+
 __global__ void __launch_bounds__(256) split_scan_kernel(const LeafTask *__restrict__ tasks,
                                                          char *__restrict__ ws, Geo g) {
-    const int l = blockIdx.z;
-    const LeafTask t = tasks[l];
-    char *sc = leaf_scalars(ws, g, l);
-    const int64_t M = g.m;
-    constexpr int KSLAB = 256;
-    if (blockIdx.y == 0) {
-        const int64_t rowblocks = (M + 255) / 256;
-        const int64_t slabs = (M + KSLAB - 1) / KSLAB;
-        if ((int64_t)blockIdx.x >= rowblocks * slabs) return;
-        int64_t i = (int64_t)(blockIdx.x % rowblocks) * 256 + threadIdx.x;
-        int64_t k0 = (int64_t)(blockIdx.x / rowblocks) * KSLAB;
-        if (i >= M) return;
-        int64_t k1 = k0 + KSLAB < M ? k0 + KSLAB : M;
-        int emax = -100000, lmin = 100000;
+    const int64_t M = g.m, per = scan_units(M), total = per * g.count;
+    const int64_t rowblocks = (M + SCAN_AROWS - 1) / SCAN_AROWS;
+    const int64_t aunits = rowblocks * ((M + SCAN_KSLAB - 1) / SCAN_KSLAB);
+    const int64_t bunits = (M + SCAN_BCOLS - 1) / SCAN_BCOLS;
+    for (int64_t it = blockIdx.x; it < total; it += gridDim.x) {
+        const int l = (int)(it / per);
+        const int64_t u = it - (int64_t)l * per;
+        const LeafTask t = tasks[l];
+        char *sc = leaf_scalars(ws, g, l);
+        if (blockIdx.y == 0) {
+            if (u >= aunits) continue;
+            const int64_t i0 = (u % rowblocks) * SCAN_AROWS + 2 * threadIdx.x;
+            const int64_t k0 = (u / rowblocks) * SCAN_KSLAB;
+            const int64_t k1 = k0 + SCAN_KSLAB < M ? k0 + SCAN_KSLAB : M;
+            if (i0 >= M) continue;
+            int e0 = -100000, l0 = 100000, e1 = -100000, l1 = 100000;
+            if ((M & 1) == 0 && ((uintptr_t)t.A & 15) == 0) {  // i0 even, M even: the pair is 16-byte aligned
 #pragma unroll 8
-        for (int64_t k = k0; k < k1; k++) {
-            double x = __ldg(t.A + i + k * M);
-            if ((unsigned long long)__double_as_longlong(x) << 1) {  // x != 0 by its encoding (an FP64 compare runs at 1/64 rate)
-                int E, lb;
-                exp_lsb(x, E, lb);
-                emax = E > emax ? E : emax;
-                lmin = lb < lmin ? lb : lmin;
-            }
-        }
-        if (emax > -100000) {
-            atomicMax(reinterpret_cast<int *>(sc + g.off_ea) + i, emax + 4096);
-            atomicMax(reinterpret_cast<int *>(sc + g.off_la) + i, 4096 - lmin);
-        }
-    } else {
-        int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        int64_t j = (int64_t)blockIdx.x * 8 + w;
-        if (j >= M) return;
-        int emax = -100000, lmin = 100000;
+                for (int64_t k = k0; k < k1; k++) {
+                    const double2 v = __ldg(reinterpret_cast<const double2 *>(t.A + i0 + k * M));
+                    scan_value(v.x, e0, l0);
+                    scan_value(v.y, e1, l1);
+                }
+            } else {
+                const bool two = i0 + 1 < M;
 #pragma unroll 8
-        for (int64_t k = lane; k < M; k += 32) {
-            double x = __ldg(t.B + k + j * M);
-            if ((unsigned long long)__double_as_longlong(x) << 1) {  // x != 0 by its encoding
-                int E, lb;
-                exp_lsb(x, E, lb);
-                emax = E > emax ? E : emax;
-                lmin = lb < lmin ? lb : lmin;
+                for (int64_t k = k0; k < k1; k++) {
+                    scan_value(__ldg(t.A + i0 + k * M), e0, l0);
+                    if (two) scan_value(__ldg(t.A + i0 + 1 + k * M), e1, l1);
+                }
             }
-        }
+            int *ea = reinterpret_cast<int *>(sc + g.off_ea), *la = reinterpret_cast<int *>(sc + g.off_la);
+            if (e0 > -100000) {
+                atomicMax(ea + i0, e0 + 4096);
+                atomicMax(la + i0, 4096 - l0);
+            }
+            if (e1 > -100000) {
+                atomicMax(ea + i0 + 1, e1 + 4096);
+                atomicMax(la + i0 + 1, 4096 - l1);
+            }
+        } else {
+            if (u >= bunits) continue;
+            const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+            const bool vec = (M & 1) == 0 && ((uintptr_t)t.B & 15) == 0;
+#pragma unroll 1
+            for (int c = 0; c < 4; c++) {
+                const int64_t j = u * SCAN_BCOLS + w * 4 + c;
+                if (j >= M) break;
+                const double *col = t.B + j * M;
+                int emax = -100000, lmin = 100000;
+                if (vec) {
+#pragma unroll 8
+                    for (int64_t k = 2 * lane; k < M; k += 64) {
+                        const double2 v = __ldg(reinterpret_cast<const double2 *>(col + k));
+                        scan_value(v.x, emax, lmin);
+                        scan_value(v.y, emax, lmin);
+                    }
+                } else {
+#pragma unroll 8
+                    for (int64_t k = lane; k < M; k += 32) scan_value(__ldg(col + k), emax, lmin);
+                }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-            lmin = min(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
-        }
-        if (lane == 0 && emax > -100000) {
-            reinterpret_cast<int *>(sc + g.off_eb)[j] = emax + 4096;
-            reinterpret_cast<int *>(sc + g.off_lb)[j] = 4096 - lmin;
+                for (int o = 16; o > 0; o >>= 1) {
+                    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+                    lmin = min(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
+                }
+                if (lane == 0 && emax > -100000) {
+                    reinterpret_cast<int *>(sc + g.off_eb)[j] = emax + 4096;
+                    reinterpret_cast<int *>(sc + g.off_lb)[j] = 4096 - lmin;
+                }
+            }
         }
     }
 }
@@ -537,17 +579,13 @@ cudaError_t launch_split_scan(const LeafTask *tasks_dev, int count, int m, Split
     Geo g = make_geo(m, count, p.scheme);
     cudaError_t e = cudaMemsetAsync(workspace, 0, g.dg_base, stream);
     if (e != cudaSuccess) return e;
-    int64_t ablocks = ((int64_t)(m + 255) / 256) * ((m + 255) / 256);
-    int64_t bblocks = (m + 7) / 8;
-    int64_t gx = ablocks > bblocks ? ablocks : bblocks;
-    for (int base = 0; base < count; base += 65535) {
-        int c = count - base < 65535 ? count - base : 65535;
-        Geo gb = g;
-        gb.sc_base = g.sc_base + (size_t)base * g.sc_per_leaf;
-        dim3 grid((unsigned)gx, 2, (unsigned)c);
-        split_scan_kernel<<<grid, 256, 0, stream>>>(tasks_dev + base, (char *)workspace, gb);
-        count_launch();
-    }
+    const int64_t M = m;
+    const int64_t aunits = ((M + SCAN_AROWS - 1) / SCAN_AROWS) * ((M + SCAN_KSLAB - 1) / SCAN_KSLAB);
+    const int64_t bunits = (M + SCAN_BCOLS - 1) / SCAN_BCOLS;
+    const int64_t items = (aunits > bunits ? aunits : bunits) * count;
+    dim3 grid((unsigned)(items < 4096 ? items : 4096), 2);
+    split_scan_kernel<<<grid, 256, 0, stream>>>(tasks_dev, (char *)workspace, g);
+    count_launch();
     return cudaGetLastError();
 }
 
