@@ -136,8 +136,6 @@ struct Op {
     bool to_caps;
     size_t split_off;  // workspace offset of the split scratch
     SplitParams sp;
-    int batch;         // K_LEAF_SPLIT: which emit_leaf_gemm call; consecutive groups of
-                       // one batch alternate two scratch buffers and pipeline their prep
 };
 
 struct Prob {
@@ -157,9 +155,6 @@ struct Builder {
     int split_group = 0;
     bool host_overlap = false;  // emit K_WAIT / K_RECORD at the top-level 'd' step
     int hybrid = 1;             // subproducts an 'h' step runs at once (desc.nproc_summa)
-    bool pipeline = false;      // two split scratch buffers per batch: prep of group g+1
-                                // overlaps the GEMM of group g
-    int batches = 0;
 
     size_t mark() const { return top; }
     void release(size_t m) { top = m; }
@@ -236,16 +231,7 @@ static void emit_leaf_gemm(Builder &b, const std::vector<Prob> &P, int64_t m) {
         // not 24 + 24 + 1 (a short last group leaves most SMs idle)
         const size_t ngroups = (P.size() + g - 1) / g;
         g = (int)((P.size() + ngroups - 1) / ngroups);
-        // with two or more groups, a second scratch buffer lets the next group's
-        // scan and slicing run while this group's GEMM does
-        const bool two = b.pipeline && ngroups >= 2;
-        const int batch = b.batches++;
-        size_t mk0 = b.mark(), buf[2] = {0, 0};
-        if (two) {
-            buf[0] = b.alloc_bytes(split_workspace_bytes((int)m, g, scheme));
-            buf[1] = b.alloc_bytes(split_workspace_bytes((int)m, g, scheme));
-        }
-        for (size_t s = 0, gi = 0; s < P.size(); s += g, gi++) {
+        for (size_t s = 0; s < P.size(); s += g) {
             size_t e = std::min(P.size(), s + g);
             std::vector<LeafTask> t;
             for (size_t i = s; i < e; i++) t.push_back({P[i].A, P[i].B, P[i].C});
@@ -254,21 +240,15 @@ static void emit_leaf_gemm(Builder &b, const std::vector<Prob> &P, int64_t m) {
             o.count = (int)t.size();
             o.m = (int)m;
             o.toff = b.table(t);
-            o.batch = two ? batch : -1;
-            if (two) {
-                o.split_off = buf[gi & 1];
-            } else {
-                size_t mk = b.mark();
-                o.split_off = b.alloc_bytes(split_workspace_bytes((int)m, o.count, scheme));
-                b.release(mk);  // scratch is dead once the launch group has run
-            }
-            // keep the peak: the allocs above already raised it
+            size_t mk = b.mark();
+            o.split_off = b.alloc_bytes(split_workspace_bytes((int)m, o.count, scheme));
+            b.release(mk);  // scratch is dead once the launch group has run
+            // keep the peak: the alloc above already raised it
             o.sp.slices = b.opt.slices;
             o.sp.diagonals = b.opt.diagonals;
             o.sp.scheme = scheme;
             b.ops.push_back(o);
         }
-        b.release(mk0);
     } else {
         std::vector<LeafTask> t;
         for (const Prob &p : P) t.push_back({p.A, p.B, p.C});
@@ -567,21 +547,15 @@ struct Planned {
 static caps_status plan(const double *A, const double *B, double *C, const caps_desc &d,
                         const char *pat, const caps_options &o, char *ws_base, Planned &pl,
                         bool host_overlap = false) {
-    // the split form's prep pipelining costs one more scratch buffer per batch
-    // of launch groups; under a budget it is dropped when that does not fit
-    for (int pipeline = 1; pipeline >= 0; pipeline--) {
-        pl.b = Builder();
-        pl.b.host_overlap = host_overlap;
-        pl.b.ws_base = ws_base;
-        pl.b.bs = d.bs;
-        pl.b.hybrid = d.nproc_summa;
-        pl.b.opt = o;
-        pl.b.pipeline = pipeline == 1 && o.form == CAPS_FORM_SPLIT;
-        std::vector<Prob> P{{A, B, C}};
-        build(pl.b, P, d.lda, d.nrec, pat);
-        pl.ws_bytes = (pl.b.peak + 255) & ~(size_t)255;
-        if (!pl.b.pipeline || o.workspace_limit <= 0 || (long long)pl.ws_bytes <= o.workspace_limit) break;
-    }
+    pl.b = Builder();
+    pl.b.host_overlap = host_overlap;
+    pl.b.ws_base = ws_base;
+    pl.b.bs = d.bs;
+    pl.b.hybrid = d.nproc_summa;
+    pl.b.opt = o;
+    std::vector<Prob> P{{A, B, C}};
+    build(pl.b, P, d.lda, d.nrec, pat);
+    pl.ws_bytes = (pl.b.peak + 255) & ~(size_t)255;
     pl.table_off = pl.ws_bytes;
     pl.total = pl.table_off + pl.b.blob.size() + 256;
     return CAPS_OK;
@@ -608,33 +582,6 @@ static caps_status upload_tables(const std::vector<uint8_t> &blob, char *dst, cu
 // `ws_base`: the workspace base its offsets refer to.
 static cudaEvent_t g_host_events[HOST_EVENTS];
 
-// Streams of the split form's pipelined launch groups, per device: the GEMMs
-// on a high-priority stream, so that their persistent CTAs are dispatched
-// ahead of the next group's prep kernels, which run on a low-priority stream
-// in what is left of each SM.
-struct PipeStreams {
-    cudaStream_t gemm = nullptr, prep = nullptr;
-    cudaEvent_t in = nullptr, prepped[2] = {nullptr, nullptr}, started = nullptr, done = nullptr;
-};
-static PipeStreams g_pipe[16];
-
-static caps_status pipe_streams(PipeStreams *&out) {
-    int dev = 0;
-    CAPS_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 16) return CAPS_ERR_UNSUPPORTED;
-    PipeStreams &p = g_pipe[dev];
-    if (!p.gemm) {
-        int least = 0, greatest = 0;
-        CAPS_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-        CAPS_CUDA_TRY(cudaStreamCreateWithPriority(&p.gemm, cudaStreamNonBlocking, greatest));
-        CAPS_CUDA_TRY(cudaStreamCreateWithPriority(&p.prep, cudaStreamNonBlocking, least));
-        for (cudaEvent_t *e : {&p.in, &p.prepped[0], &p.prepped[1], &p.started, &p.done})
-            CAPS_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
-    }
-    out = &p;
-    return CAPS_OK;
-}
-
 static caps_status launch_ops(const std::vector<Op> &ops, char *tables, char *ws_base, cudaStream_t s,
                               double *phase_time, KernelTiming *kt) {
     struct Rec {
@@ -648,84 +595,10 @@ static caps_status launch_ops(const std::vector<Op> &ops, char *tables, char *ws
         cudaEventCreate(&e);
         cudaEventRecord(e, s);
     };
-    auto launch_prep = [&](const Op &o, cudaStream_t st) {
-        const LeafTask *t = reinterpret_cast<const LeafTask *>(tables + o.toff);
-        void *ws = ws_base + o.split_off;
-        // scan + prep are timed with the multiply phase but not as GEMM
-        Rec pre{nullptr, nullptr, PH_MUL, false, 0.0};
-        const bool timed = phase_time || kt;
-        if (timed) {
-            cudaEventCreate(&pre.e0);
-            cudaEventRecord(pre.e0, st);
-        }
-        cudaError_t err = launch_split_scan(t, o.count, o.m, o.sp, ws, st);
-        if (err == cudaSuccess) err = launch_split_prep(t, o.count, o.m, o.sp, ws, st);
-        if (timed) {
-            cudaEventCreate(&pre.e1);
-            cudaEventRecord(pre.e1, st);
-            recs.push_back(pre);
-        }
-        return err;
-    };
-    PipeStreams *pipe = nullptr;
-    for (size_t oi = 0; oi < ops.size(); oi++) {
-        const Op &o = ops[oi];
+    for (const Op &o : ops) {
         const bool timed = phase_time || kt;
         Rec r{nullptr, nullptr, PH_ADD, false, 0.0};
         cudaError_t err = cudaSuccess;
-        if (o.kind == K_LEAF_SPLIT && o.batch >= 0) {
-            // group g of a pipelined batch: its prep ran on the prep stream
-            // (launched with group g-1's GEMM, or here for the first group);
-            // its GEMM runs on the GEMM stream, and the next group's prep is
-            // launched to run beside it, into the other scratch buffer
-            const bool first = oi == 0 || ops[oi - 1].kind != K_LEAF_SPLIT || ops[oi - 1].batch != o.batch;
-            const bool last = oi + 1 == ops.size() || ops[oi + 1].kind != K_LEAF_SPLIT || ops[oi + 1].batch != o.batch;
-            int gi = 0;  // group index within the batch
-            for (size_t k = oi; k > 0 && ops[k - 1].kind == K_LEAF_SPLIT && ops[k - 1].batch == o.batch; k--) gi++;
-            if (first) {
-                CAPS_TRY(pipe_streams(pipe));
-                CAPS_CUDA_TRY(cudaEventRecord(pipe->in, s));
-                CAPS_CUDA_TRY(cudaStreamWaitEvent(pipe->prep, pipe->in, 0));
-                err = launch_prep(o, pipe->prep);
-                if (err == cudaSuccess) err = cudaEventRecord(pipe->prepped[0], pipe->prep);
-                if (err != cudaSuccess) {
-                    note_cuda_error(err, "kernel launch");
-                    return CAPS_ERR_CUDA;
-                }
-            }
-            CAPS_CUDA_TRY(cudaStreamWaitEvent(pipe->gemm, pipe->prepped[gi & 1], 0));
-            // complete once the previous group's GEMM is done and this group is prepared
-            CAPS_CUDA_TRY(cudaEventRecord(pipe->started, pipe->gemm));
-            if (timed) {
-                cudaEventCreate(&r.e0);
-                cudaEventRecord(r.e0, pipe->gemm);
-            }
-            err = launch_split_gemm(reinterpret_cast<const LeafTask *>(tables + o.toff), o.count, o.m, o.sp,
-                                    ws_base + o.split_off, reinterpret_cast<unsigned *>(g_status.ptr), pipe->gemm);
-            if (err == cudaSuccess && timed) {
-                cudaEventCreate(&r.e1);
-                cudaEventRecord(r.e1, pipe->gemm);
-                r.phase = PH_MUL;
-                r.gemm = true;
-                r.m3 = (double)o.count * o.m * (double)o.m * o.m;
-                recs.push_back(r);
-            }
-            if (err == cudaSuccess && !last) {
-                // the next group's buffer was last read by the GEMM before this one
-                err = cudaStreamWaitEvent(pipe->prep, pipe->started, 0);
-                if (err == cudaSuccess) err = launch_prep(ops[oi + 1], pipe->prep);
-                if (err == cudaSuccess) err = cudaEventRecord(pipe->prepped[(gi + 1) & 1], pipe->prep);
-            }
-            if (err == cudaSuccess && last) {
-                err = cudaEventRecord(pipe->done, pipe->gemm);
-                if (err == cudaSuccess) err = cudaStreamWaitEvent(s, pipe->done, 0);
-            }
-            if (err != cudaSuccess) {
-                note_cuda_error(err, "kernel launch");
-                return CAPS_ERR_CUDA;
-            }
-            continue;
-        }
         switch (o.kind) {
             case K_EW:
                 if (timed) ev_begin(r.e0);

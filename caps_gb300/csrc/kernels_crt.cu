@@ -218,11 +218,12 @@ __global__ void crt_resolve_kernel(char *__restrict__ ws, Geo g, SplitParams p) 
 // one thread = one column x 8 k, a block = half of a 256 x 16 tile.
 __device__ __forceinline__ void crt_slice_tile(const LeafTask *__restrict__ tasks, char *__restrict__ ws,
                                                const Geo &g, const SplitHdr *h, int L, int leaf, int64_t tile,
-                                               int side, int tid) {
+                                               int side) {
     const LeafTask t = tasks[leaf];
     const char *sc = leaf_scalars(ws, g, leaf);
     char *pl = leaf_digits(ws, g, leaf);
     const int64_t M = g.m;
+    const int tid = threadIdx.x;
     const int kg = tid >> 7;  // which 8 of the tile's 16 k
     int64_t idx, k0, sk;      // row of A / column of B, first k, stride between k
     const double *src;
@@ -289,10 +290,7 @@ __device__ __forceinline__ void crt_slice_tile(const LeafTask *__restrict__ task
 
 // Grid-stride over (leaf, tile), so that the launch is cheap when the digit
 // scheme runs and this kernel returns at once.  blockIdx.y: A (0) or B (1).
-// A block of 128 threads does the work of 256 (thread indexes t and t + 128
-// in turn): 128 x 56 registers fit beside the residue GEMM's CTA on an SM,
-// so the next launch group's slicing runs while this group's GEMM does.
-__global__ void __launch_bounds__(128) crt_slice_kernel(const LeafTask *__restrict__ tasks,
+__global__ void __launch_bounds__(256) crt_slice_kernel(const LeafTask *__restrict__ tasks,
                                                         char *__restrict__ ws, Geo g) {
     const SplitHdr *h = reinterpret_cast<const SplitHdr *>(ws);
     if (!h->residues) return;  // the digit scheme runs
@@ -301,9 +299,7 @@ __global__ void __launch_bounds__(128) crt_slice_kernel(const LeafTask *__restri
     const int64_t per = atiles > bhalves ? atiles : bhalves;
     const int64_t total = per * g.count;
     for (int64_t it = blockIdx.x; it < total; it += gridDim.x)
-#pragma unroll 1
-        for (int half = 0; half < 2; half++)
-            crt_slice_tile(tasks, ws, g, h, L, (int)(it / per), it % per, blockIdx.y, threadIdx.x + 128 * half);
+        crt_slice_tile(tasks, ws, g, h, L, (int)(it / per), it % per, blockIdx.y);
 }
 
 // ---------------------------------------------------------------- CRT reconstruction
@@ -751,7 +747,7 @@ cudaError_t launch_crt_slice(const LeafTask *tasks_dev, int count, int m, SplitP
     const int64_t atiles = (int64_t)g.mtiles * g.nks, bhalves = (int64_t)g.rtiles * g.nks * 2;
     const int64_t items = (atiles > bhalves ? atiles : bhalves) * count;
     dim3 grid((unsigned)(items < 4096 ? items : 4096), 2);
-    crt_slice_kernel<<<grid, 128, 0, stream>>>(tasks_dev, (char *)workspace, g);
+    crt_slice_kernel<<<grid, 256, 0, stream>>>(tasks_dev, (char *)workspace, g);
     count_launch();
     return cudaGetLastError();
 }

@@ -228,11 +228,12 @@ __device__ __forceinline__ uint32_t bf16_of_digit(int d) {
 // 128 x 16 tile.  B side: one thread = one column x 8 k; 256 threads = two
 // 64 x 16 tiles.
 __device__ __forceinline__ void split_slice_tile(const LeafTask *__restrict__ tasks, int m, char *__restrict__ ws,
-                                                 const Geo &g, int s, int leaf, int64_t tile, int side, int tid) {
+                                                 const Geo &g, int s, int leaf, int64_t tile, int side) {
     const LeafTask t = tasks[leaf];
     char *sc = leaf_scalars(ws, g, leaf);
     char *dg = leaf_digits(ws, g, leaf);
     const int64_t M = m;
+    const int tid = threadIdx.x;
     const int64_t atiles = (int64_t)g.mtiles * g.nks;
     if (side == 0) {
         if (tile >= atiles) return;
@@ -295,9 +296,7 @@ __device__ __forceinline__ void split_slice_tile(const LeafTask *__restrict__ ta
 
 // Grid-stride over (leaf, tile), so that the launch is cheap when the residue
 // scheme runs and this kernel returns at once.  blockIdx.y: A (0) or B (1).
-// A block of 128 threads does the work of 256 (thread indexes t and t + 128
-// in turn), small enough to run beside a GEMM CTA on an SM.
-__global__ void __launch_bounds__(128) split_slice_kernel(const LeafTask *__restrict__ tasks, int m,
+__global__ void __launch_bounds__(256) split_slice_kernel(const LeafTask *__restrict__ tasks, int m,
                                                           char *__restrict__ ws, Geo g, SplitParams p) {
     const SplitHdr *h = reinterpret_cast<const SplitHdr *>(ws);
     if (h->residues) return;  // the residue scheme runs
@@ -307,9 +306,7 @@ __global__ void __launch_bounds__(128) split_slice_kernel(const LeafTask *__rest
     const int64_t per = atiles > btiles2 ? atiles : btiles2;
     const int64_t total = per * g.count;
     for (int64_t it = blockIdx.x; it < total; it += gridDim.x)
-#pragma unroll 1
-        for (int half = 0; half < 2; half++)
-            split_slice_tile(tasks, m, ws, g, s, (int)(it / per), it % per, blockIdx.y, threadIdx.x + 128 * half);
+        split_slice_tile(tasks, m, ws, g, s, (int)(it / per), it % per, blockIdx.y);
 }
 
 // ---------------------------------------------------------------- gemm
@@ -615,7 +612,7 @@ cudaError_t launch_split_prep(const LeafTask *tasks_dev, int count, int m, Split
         int64_t btiles2 = ((int64_t)g.ntiles * g.nks + 1) / 2;
         int64_t items = (atiles > btiles2 ? atiles : btiles2) * count;
         dim3 grid((unsigned)(items < 4096 ? items : 4096), 2);
-        split_slice_kernel<<<grid, 128, 0, stream>>>(tasks_dev, m, ws, g, p);
+        split_slice_kernel<<<grid, 256, 0, stream>>>(tasks_dev, m, ws, g, p);
         count_launch();
     }
     return cudaGetLastError();
