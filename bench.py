@@ -655,6 +655,8 @@ def main():
     for _ in range(args.steps):
         cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices, scheme=args.scheme)
     t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
+    # the copy rates again: on a shared host they can drop while the leg runs
+    copy_bw_after = pinned_copy_bandwidth(hA, A, stream)
     barrier(world)
 
     # ---- plain FP64 Strassen of the same multiply, and the errors of both
@@ -756,6 +758,7 @@ def main():
             "e2e": {"value": world * 2.0 * n ** 3 / t_e2e / 1e12, "unit": "TFLOP/s",
                     "h2d_bytes_per_step": 2 * n * n * 8, "d2h_bytes_per_step": n * n * 8,
                     "ms_per_step": t_e2e * 1e3, "pinned_copy_gbs": copy_bw,
+                    "pinned_copy_gbs_after_e2e": copy_bw_after,
                     "pinned_copy_gbs_after_error_checks": out.get("copy_bw_late"),
                     "api": "caps_multiply_host, pinned host buffers, no pattern given: top level 'd' + %s "
                            "with copies overlapped" % e2e_pattern[1:]},
