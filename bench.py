@@ -342,12 +342,13 @@ def run_batched512(args, world, rank, local):
         for _ in range(max(1, args.warmup if form == "split" else 1)):  # first call tunes and captures
             cg.multiply_batched(As, Bs, Cs, sizes, form=form)
         barrier(world)
-        t0 = time.perf_counter()
-        for _ in range(steps):
-            cg.multiply_batched(As, Bs, Cs, sizes, form=form)  # synchronises
-        t = max_over_ranks((time.perf_counter() - t0) / steps, world)
+        with ClockSampler(local) as clk:
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                cg.multiply_batched(As, Bs, Cs, sizes, form=form)  # synchronises
+            t = max_over_ranks((time.perf_counter() - t0) / steps, world)
         res[form] = {"value": world * eff / t / 1e12, "ms_per_step": t * 1e3, "steps": steps,
-                     "graph_kernels": cg.counters()["kernel_launches"]}
+                     "graph_kernels": cg.counters()["kernel_launches"], "clocks": clk.summary()}
         if rank == 0:  # error of three instances against binary128
             res[form]["error"] = {
                 str(sizes[i]): sampled_error(Cs[i].cpu().numpy(), As[i].cpu().numpy(), Bs[i].cpu().numpy(),
@@ -361,7 +362,7 @@ def run_batched512(args, world, rank, local):
                                       "execution": "per-size autotuned depth/pattern, CUDA graph replay"},
                                      split=res["split"], plain_fp64=res["plain"],
                                      split_vs_plain=res["split"]["value"] / res["plain"]["value"],
-                                     autotune=cg.autotune_table(),
+                                     autotune=cg.autotune_table(), clocks=res["split"]["clocks"],
                                      gpu_launches=res["split"]["graph_kernels"] * args.steps)), flush=True)
 
 
