@@ -268,7 +268,29 @@ __device__ __forceinline__ void crt_slice_tile(const LeafTask *__restrict__ task
     Limbs x[8];
 #pragma unroll
     for (int e = 0; e < 8; e++) x[e] = limbs14(scaled_round(v[e], f));
-    if (side == 0) {
+    if (L == LMAX) {
+        // float data always needs every modulus: unrolled, the FMAs take the
+        // constants straight from the constant bank
+        if (side == 0) {
+#pragma unroll
+            for (int l = 0; l < LMAX; l++) {
+                uint32_t w[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    w[q] = pack_bf16x2(residue_y_f32(x[2 * q], LMAX, l), residue_y_f32(x[2 * q + 1], LMAX, l));
+                *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
+            }
+        } else {
+#pragma unroll
+            for (int l = 0; l < LMAX; l++) {
+                uint32_t w[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    w[q] = pack_bf16x2(residue_f32(x[2 * q], l), residue_f32(x[2 * q + 1], l));
+                *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
+            }
+        }
+    } else if (side == 0) {
 #pragma unroll 1
         for (int l = 0; l < L; l++) {
             uint32_t w[4];
