@@ -383,14 +383,15 @@ def run_int32768(args, world, rank, local):
     res = {}
     for form in ("split", "plain"):
         steps = args.steps if form == "split" else 1
-        cg.multiply(A, B, C, d, pat, form=form, workspace_limit=budget)
+        sch = args.scheme if form == "split" else "auto"
+        cg.multiply(A, B, C, d, pat, form=form, workspace_limit=budget, scheme=sch)
         torch.cuda.synchronize()
         cg.set_phase_timing(True)
         t_tot, add_t, add_b = 0.0, 0.0, 0
         for _ in range(steps):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
-            cg.multiply(A, B, C, d, pat, form=form, workspace_limit=budget)
+            cg.multiply(A, B, C, d, pat, form=form, workspace_limit=budget, scheme=sch)
             e1.record()
             torch.cuda.synchronize()
             c = cg.counters()
@@ -415,8 +416,10 @@ def run_int32768(args, world, rank, local):
             ref = int((Am[:, i].to(torch.int64) * Bm[j].to(torch.int64)).sum().item())
             exact += int(float(Cm[j, i].item()) == float(ref))
         del y, Ac, Bc
+        cnt = cg.counters()
         res[form] = {"value": 2.0 * n ** 3 / t / 1e12, "ms_per_step": t * 1e3, "steps": steps,
-                     "bit_exact_sampled": "%d/64" % exact,
+                     "bit_exact_sampled": "%d/64" % exact, "leaf_gemm_ms": cnt["time_leaf_gemm"] * 1e3,
+                     "split_moduli": cnt["split_moduli"], "split_slices": cnt["split_slices"],
                      "additions_hbm_gbs": add_b / add_t / 1e9 if add_t > 0 else None,
                      "workspace_bytes": cg.counters()["workspace_peak_bytes"]}
     if rank == 0:

@@ -12,7 +12,7 @@
 //     |A'| <= 2^t_a, |B'| <= 2^t_b, exact when the data needs <= t bits.
 //  2. resolve: the fewest moduli L whose product M_L exceeds
 //     2 * K * 2^(t_a + t_b) (so C' = A'B' is fixed by its residues), and the
-//     scheme: residues when L + 3 < the digit scheme's digit-pair count.
+//     scheme: residues wherever they fit (K <= 2048), digits otherwise.
 //  3. slice:   residues of A', B' modulo the pairwise coprime moduli
 //     p_l in {181, 180, 179, 173, ...} (balanced, |r| <= 90, exact in bf16),
 //     written as pre-tiled UMMA canonical K-major planes like the digits.
@@ -112,14 +112,6 @@ void build_tables(CrtTables &t) {
     }
 }
 
-__device__ __forceinline__ int digit_pairs(int s, int nd) {
-    int n = 0;
-    for (int a = 1; a <= s; a++) {
-        int j = s < nd + 1 - a ? s : nd + 1 - a;
-        n += j > 0 ? j : 0;
-    }
-    return n;
-}
 
 // 1.5 * 2^23: adding it to a float of magnitude below 2^22 rounds that float
 // to an integer (one rounding of the exact sum), and the low bits of the
@@ -201,7 +193,10 @@ __global__ void crt_resolve_kernel(char *__restrict__ ws, Geo g, SplitParams p) 
         const int need = ta + tb + kb + 1;  // K 2^(ta+tb) < M_L / 2
         L = 1;
         while (L <= LMAX && c_crt.lg[L] < need) L++;
-        if (L <= LMAX && (p.scheme == SCHEME_RESIDUES || L + 3 < digit_pairs(s, nd))) residues = 1;
+        // wherever the residues fit they are the faster cut, integer data
+        // included: the digit GEMM's per-chunk drain of its diagonal
+        // accumulators costs about as much at one digit as at eight
+        if (L <= LMAX) residues = 1;
     }
     h->ta = ta;
     h->tb = tb;

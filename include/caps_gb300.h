@@ -58,9 +58,10 @@ typedef enum caps_form {
 /* How the split form cuts the base-case operands.  Both scale each row of A
  * and column of B by a power of two into integers of up to 55 bits. */
 typedef enum caps_split_scheme {
-    CAPS_SPLIT_AUTO = 0,     /* per launch group of leaves, from the data: residues
-                                when they need fewer tensor-core products (float
-                                data), digits otherwise (integer-like data) */
+    CAPS_SPLIT_AUTO = 0,     /* per launch group of leaves: residues wherever the
+                                leaves fit them (up to 2048; float and integer
+                                data alike, the moduli counted from the data),
+                                digits for larger leaves */
     CAPS_SPLIT_DIGITS = 1,   /* balanced base-128 digits, one product per kept
                                 digit pair (36 for float data) */
     CAPS_SPLIT_RESIDUES = 2  /* residues modulo up to 17 coprime moduli <= 181,

@@ -49,13 +49,17 @@ def test_split_leaf_bitexact_forced_digits(caps, oracle_mod, cuda, s, nd):
     assert np.array_equal(C, ref)
 
 
+@pytest.mark.parametrize("scheme", ["auto", "digits"])
 @pytest.mark.parametrize("m,lim", [(256, 1024), (640, 9), (2048, 1024)])
-def test_split_leaf_integers_exact(caps, oracle_mod, cuda, m, lim):
+def test_split_leaf_integers_exact(caps, oracle_mod, cuda, m, lim, scheme):
     rng = np.random.default_rng(m)
     A = rng.integers(-lim, lim + 1, (m, m)).astype(np.float64)
     B = rng.integers(-lim, lim + 1, (m, m)).astype(np.float64)
-    C, cnt = _leaf(caps, cuda, A, B)
-    assert cnt["split_slices"] <= 4
+    C, cnt = _leaf(caps, cuda, A, B, scheme=scheme)
+    if scheme == "digits":
+        assert 0 < cnt["split_slices"] <= 4
+    else:
+        assert 0 < cnt["split_moduli"] <= 8
     assert np.array_equal(C, (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64))
 
 
@@ -197,8 +201,9 @@ def test_residue_leaf_integers_exact(caps, oracle_mod, cuda, m, lim):
 
 
 def test_auto_scheme_choice(caps, oracle_mod, cuda):
-    """Float data: residues (16-17 products instead of 36 digit pairs);
-    small integers: digits (1 to 3 digit pairs)."""
+    """Residues wherever the leaves fit them (K <= 2048), integer data
+    included: float data take 16-17 moduli, 11-bit integers 5; above 2048
+    the digits run."""
     m = 512
     rng = np.random.default_rng(3)
     A = rng.uniform(-1, 1, (m, m))
@@ -209,7 +214,16 @@ def test_auto_scheme_choice(caps, oracle_mod, cuda):
     Ai = rng.integers(-1024, 1025, (m, m)).astype(np.float64)
     Bi = rng.integers(-1024, 1025, (m, m)).astype(np.float64)
     C, cnt = _leaf(caps, cuda, Ai, Bi)
+    Cr, t = _residue_ref(oracle_mod, Ai, Bi)
+    assert cnt["split_moduli"] == expected_moduli(t[0], t[1], m) <= 5 and cnt["split_slices"] == 0
+    assert np.array_equal(C, Cr)
+    assert np.array_equal(C, (Ai.astype(np.int64) @ Bi.astype(np.int64)).astype(np.float64))
+    m = 2064
+    Ai = rng.integers(-1024, 1025, (m, m)).astype(np.float64)
+    Bi = rng.integers(-1024, 1025, (m, m)).astype(np.float64)
+    C, cnt = _leaf(caps, cuda, Ai, Bi)
     assert cnt["split_moduli"] == 0 and cnt["split_slices"] == 2
+    assert np.array_equal(C, (Ai.astype(np.int64) @ Bi.astype(np.int64)).astype(np.float64))
 
 
 def test_residue_scheme_falls_back_to_digits_above_2048(caps, oracle_mod, cuda):
