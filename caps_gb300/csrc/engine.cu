@@ -1193,7 +1193,8 @@ caps_status caps_leaf_gemm_dev(const double *A, const double *B, double *C, int 
 // the multiply writes C directly and C is never read (dgemm's beta = 0 rule,
 // mult.cpp:91-98).
 static caps_status chol_mult_locked(double *C, const double *A, const double *B, int n, int x, int r,
-                                    double alpha, const char *pattern, const caps_options &o, cudaStream_t s) {
+                                    double alpha, const char *pattern, const caps_options &o, cudaStream_t s,
+                                    cudaEvent_t c_ready = nullptr) {
     if (!A || !B || !C) return CAPS_ERR_ARG;
     if (x != 1) {
         g_last_err = "mult: x > 1 process groups need more than one rank";
@@ -1210,7 +1211,10 @@ static caps_status chol_mult_locked(double *C, const double *A, const double *B,
     double *prod = direct ? C : (double *)(g_chol.ptr + slot);
     CAPS_CUDA_TRY(launch_rec_transpose(B, nbt, n, r, true, s));
     CAPS_TRY(multiply_dev_locked(A, nbt, prod, d, pattern, o, s, true));
-    if (!direct) CAPS_CUDA_TRY(launch_scale_add(C, prod, alpha, (int64_t)n * n, s));
+    if (!direct) {
+        if (c_ready) CAPS_CUDA_TRY(cudaStreamWaitEvent(s, c_ready, 0));  // C's copy, made beside the multiply
+        CAPS_CUDA_TRY(launch_scale_add(C, prod, alpha, (int64_t)n * n, s));
+    }
     return CAPS_OK;
 }
 
@@ -1229,10 +1233,32 @@ caps_status caps_chol_mult_host(double *C, const double *A, const double *B, int
     CAPS_TRY(ensure(g_io, 3 * slot));
     double *dA = (double *)g_io.ptr, *dB = (double *)(g_io.ptr + slot), *dC = (double *)(g_io.ptr + 2 * slot);
     cudaStream_t s = 0;
-    CAPS_CUDA_TRY(cudaMemcpyAsync(dA, A, nn, cudaMemcpyHostToDevice, s));
+    // C is needed only by the final scale-add: it is copied on a side stream
+    // while the product runs
+    static cudaStream_t cs = nullptr;
+    static cudaEvent_t start = nullptr, c_ready = nullptr;
+    if (!cs) {
+        CAPS_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        CAPS_CUDA_TRY(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+        CAPS_CUDA_TRY(cudaEventCreateWithFlags(&c_ready, cudaEventDisableTiming));
+    }
+    const bool copy_c = alpha != 0.0;
     CAPS_CUDA_TRY(cudaMemcpyAsync(dB, B, nn, cudaMemcpyHostToDevice, s));
-    if (alpha != 0.0) CAPS_CUDA_TRY(cudaMemcpyAsync(dC, C, nn, cudaMemcpyHostToDevice, s));
-    CAPS_TRY(chol_mult_locked(dC, dA, dB, n, x, r, alpha, pattern, opts_or_default(opt), s));
+    CAPS_CUDA_TRY(cudaMemcpyAsync(dA, A, nn, cudaMemcpyHostToDevice, s));
+    if (copy_c) {
+        // after A and B are in (the copies share the host link) and after earlier
+        // work on s, so dC is free
+        CAPS_CUDA_TRY(cudaEventRecord(start, s));
+        CAPS_CUDA_TRY(cudaStreamWaitEvent(cs, start, 0));
+        CAPS_CUDA_TRY(cudaMemcpyAsync(dC, C, nn, cudaMemcpyHostToDevice, cs));
+        CAPS_CUDA_TRY(cudaEventRecord(c_ready, cs));
+    }
+    caps_status st = chol_mult_locked(dC, dA, dB, n, x, r, alpha, pattern, opts_or_default(opt), s,
+                                      copy_c ? c_ready : nullptr);
+    if (st != CAPS_OK) {
+        cudaStreamSynchronize(cs);
+        return st;
+    }
     CAPS_CUDA_TRY(cudaMemcpyAsync(C, dC, nn, cudaMemcpyDeviceToHost, s));
     CAPS_CUDA_TRY(cudaStreamSynchronize(s));
     return CAPS_OK;
