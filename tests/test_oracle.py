@@ -97,7 +97,7 @@ def test_oracle_bitexact_vs_live_reference(oracle_mod):
 
 
 def test_counters_match_reference_counts(oracle_mod):
-    """additions/multiplications as counters.cpp counts them (SURVEY: 1.463e9 adds at n=8192, r=3)."""
+    """additions/multiplications as counters.cpp counts them (1.463e9 additions at n=8192, r=3)."""
     import caps_gb300
     f = caps_gb300.flop_counts(8192, 3)
     m = 1024
