@@ -104,6 +104,41 @@ def test_reference_drivers_link_unmodified_against_library(caps, tmp_path):
         assert r.returncode == 0, r.stdout
 
 
+@pytest.mark.skipif(not os.path.isfile("/root/reference/cholesky/test-mult.cpp"), reason="reference sources absent")
+def test_cholesky_test_mult_links_against_library(caps, tmp_path):
+    """The Cholesky subproject's own test-mult.cpp, with its sizes /
+    communication / counters / library objects but without mult.o, links
+    against libcaps_gb300.so: its mult() call resolves to the library's."""
+    shim = os.path.join(ROOT, "oracle", "ref_shim")
+    ref = "/root/reference/cholesky"
+    libdir = os.path.dirname(caps.LIB_PATH)
+    import numpy
+    npl = os.path.realpath(os.path.join(os.path.dirname(numpy.__file__), os.pardir, "numpy.libs"))
+    blas = [os.path.join(npl, f) for f in (os.listdir(npl) if os.path.isdir(npl) else [])
+            if f.startswith("libscipy_openblas64_")]
+    if not blas:
+        pytest.skip("numpy's OpenBLAS not found (test-mult checks itself with dgemm)")
+    objs = []
+    for src in ("test-mult", "sizes", "communication", "counters", "library"):
+        o = str(tmp_path / (src + ".o"))
+        cmd = ["g++", "-O1", "-w", "-fopenmp", "-DNUM_THREADS=1", "-include", os.path.join(shim, "mpi.h"),
+               "-I" + shim, "-I" + ref, "-c", os.path.join(ref, src + ".cpp"), "-o", o]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        assert r.returncode == 0, r.stdout
+        objs.append(o)
+    bo = str(tmp_path / "blas_lp64.o")
+    r = subprocess.run(["gcc", "-O1", "-c", os.path.join(shim, "blas_lp64.c"), "-o", bo],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout
+    out = str(tmp_path / "test-mult")
+    cmd = (["g++", "-fopenmp", "-o", out] + objs + [bo, blas[0], "-Wl,-rpath," + npl, "-L" + libdir, "-lcaps_gb300",
+                                                    "-Wl,-rpath," + libdir])
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout
+    syms = subprocess.run(["nm", out], stdout=subprocess.PIPE, text=True).stdout
+    assert " U _Z4multPdS_S_iiid" in syms  # left to the shared library
+
+
 def test_hybrid_step_workspace_between_d_and_b(caps):
     """An 'h' step with factor k (desc.nproc_summa) holds the workspace of k
     concurrent subproducts: more than 'd', less than 'b'; k = 1 runs as 'd'."""
