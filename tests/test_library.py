@@ -172,3 +172,9 @@ def test_chol_mult_validation_before_any_device_work(caps):
     assert call(p, p, p, 0, 1, 0) == 2
     assert call(p, p, p, 64, 1, 2, b"dx") == 1
     assert call(None, p, p, 64, 1, 2) == 8
+    # the host entry point checks its pointers and size before any copy
+    dp = ctypes.POINTER(ctypes.c_double)
+    assert L.caps_chol_mult_host(None, None, None, 64, 1, 2, 1.0, None, ctypes.byref(opt)) == 8
+    buf = (ctypes.c_double * 4)()
+    hp = ctypes.cast(buf, dp)
+    assert L.caps_chol_mult_host(hp, hp, hp, 0, 1, 0, 1.0, None, ctypes.byref(opt)) == 2
