@@ -56,8 +56,11 @@ def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(OBJ, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     os.makedirs(BINDIR, exist_ok=True)
-    headers = [os.path.join(CSRC, "common.cuh"), os.path.join(ROOT, "include", "caps_gb300.h"),
-               os.path.join(ROOT, "include", "caps_compat.h")]
+    # every translation unit is rebuilt when any shared header changes (the
+    # split kernels' tile constants, wait limit and descriptors live in
+    # split_common.cuh)
+    headers = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h")))
+    headers += [os.path.join(ROOT, "include", "caps_gb300.h"), os.path.join(ROOT, "include", "caps_compat.h")]
     nv = nvcc()
     jobs = []
     objs = []

@@ -2,9 +2,17 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <mutex>
+
 #include "../../include/caps_gb300.h"
 
 namespace caps {
+
+// The lock every entry point holds while it plans, launches and reads back:
+// the engine's caches, the kernels' per-device set-up and the status word
+// are shared by all calls in the process.
+std::recursive_mutex &library_mutex();
 
 // Records the CUDA error text for caps_last_cuda_error().
 void note_cuda_error(cudaError_t e, const char *where);

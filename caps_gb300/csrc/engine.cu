@@ -23,6 +23,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -32,6 +33,7 @@ namespace caps {
 // ------------------------------------------------------------------ state
 static thread_local std::string g_last_err;
 static std::recursive_mutex g_mu;
+std::recursive_mutex &library_mutex() { return g_mu; }
 static long long g_launches = 0;
 static caps_counters g_counters;
 static int g_fail_allocs = 0;
@@ -578,9 +580,43 @@ static caps_status upload_tables(const std::vector<uint8_t> &blob, char *dst, cu
     return CAPS_OK;
 }
 
+// Streams and events of the host entry points, one set per device (a call
+// made with another device current must not record on the first device's
+// stream or events).  Created on first use on a device, destroyed by
+// caps_release_cache.
+struct HostSide {
+    int device = -1;
+    cudaStream_t copy = nullptr;             // H2D / D2H copies beside the multiply
+    cudaEvent_t start = nullptr;             // earlier work on the caller's stream is done
+    cudaEvent_t c_ready = nullptr;           // caps_chol_mult_host: C is on the device
+    cudaEvent_t events[HOST_EVENTS] = {};    // caps_multiply_host: quadrant hand-offs
+};
+static std::deque<HostSide> g_host_sides;  // deque: elements stay put as devices are added
+
+static caps_status host_side(HostSide **out) {
+    int dev = 0;
+    CAPS_CUDA_TRY(cudaGetDevice(&dev));
+    for (HostSide &h : g_host_sides)
+        if (h.device == dev) {
+            *out = &h;
+            return CAPS_OK;
+        }
+    HostSide h;
+    h.device = dev;
+    CAPS_CUDA_TRY(cudaStreamCreateWithFlags(&h.copy, cudaStreamNonBlocking));
+    CAPS_CUDA_TRY(cudaEventCreateWithFlags(&h.start, cudaEventDisableTiming));
+    CAPS_CUDA_TRY(cudaEventCreateWithFlags(&h.c_ready, cudaEventDisableTiming));
+    for (int i = 0; i < HOST_EVENTS; i++) CAPS_CUDA_TRY(cudaEventCreateWithFlags(&h.events[i], cudaEventDisableTiming));
+    g_host_sides.push_back(h);
+    *out = &g_host_sides.back();
+    return CAPS_OK;
+}
+
+// The quadrant events of the host call in progress (K_WAIT / K_RECORD ops).
+static cudaEvent_t *g_host_events = nullptr;
+
 // Launches a plan's ops.  `tables`: the plan's task tables on the device;
 // `ws_base`: the workspace base its offsets refer to.
-static cudaEvent_t g_host_events[HOST_EVENTS];
 
 static caps_status launch_ops(const std::vector<Op> &ops, char *tables, char *ws_base, cudaStream_t s,
                               double *phase_time, KernelTiming *kt) {
@@ -1121,14 +1157,11 @@ caps_status caps_multiply_host(const double *A, const double *B, double *C, caps
         CAPS_CUDA_TRY(cudaStreamSynchronize(s));
         return CAPS_OK;
     }
-    static cudaStream_t cs = nullptr;
-    static cudaEvent_t start = nullptr;
-    if (!cs) {
-        CAPS_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-        CAPS_CUDA_TRY(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
-        for (int i = 0; i < HOST_EVENTS; i++)
-            CAPS_CUDA_TRY(cudaEventCreateWithFlags(&g_host_events[i], cudaEventDisableTiming));
-    }
+    HostSide *hs = nullptr;
+    CAPS_TRY(host_side(&hs));
+    cudaStream_t cs = hs->copy;
+    cudaEvent_t start = hs->start;
+    g_host_events = hs->events;
     const size_t q = nn / 4;  // quadrant bytes: X11, X21, X12, X22 at 0, q, 2q, 3q
     auto h2d = [&](double *dst, const double *src, int quad) {
         return cudaMemcpyAsync((char *)dst + quad * q, (const char *)src + quad * q, q, cudaMemcpyHostToDevice, cs);
@@ -1235,13 +1268,10 @@ caps_status caps_chol_mult_host(double *C, const double *A, const double *B, int
     cudaStream_t s = 0;
     // C is needed only by the final scale-add: it is copied on a side stream
     // while the product runs
-    static cudaStream_t cs = nullptr;
-    static cudaEvent_t start = nullptr, c_ready = nullptr;
-    if (!cs) {
-        CAPS_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-        CAPS_CUDA_TRY(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
-        CAPS_CUDA_TRY(cudaEventCreateWithFlags(&c_ready, cudaEventDisableTiming));
-    }
+    HostSide *hs = nullptr;
+    CAPS_TRY(host_side(&hs));
+    cudaStream_t cs = hs->copy;
+    cudaEvent_t start = hs->start, c_ready = hs->c_ready;
     const bool copy_c = alpha != 0.0;
     CAPS_CUDA_TRY(cudaMemcpyAsync(dB, B, nn, cudaMemcpyHostToDevice, s));
     CAPS_CUDA_TRY(cudaMemcpyAsync(dA, A, nn, cudaMemcpyHostToDevice, s));
@@ -1366,6 +1396,18 @@ void caps_release_cache(void) {
     g_pinned.ptr = nullptr;
     g_pinned.size = 0;
     g_pinned.pending = false;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    for (HostSide &h : g_host_sides) {
+        cudaSetDevice(h.device);
+        cudaStreamDestroy(h.copy);
+        cudaEventDestroy(h.start);
+        cudaEventDestroy(h.c_ready);
+        for (int i = 0; i < HOST_EVENTS; i++) cudaEventDestroy(h.events[i]);
+    }
+    g_host_sides.clear();
+    g_host_events = nullptr;
+    cudaSetDevice(cur);
 }
 
 }  // extern "C"

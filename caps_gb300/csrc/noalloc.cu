@@ -16,16 +16,18 @@
 //   - every GPU that loads the library holds the array (8.5 MiB) until exit;
 //   - all calls share the array and it keeps the last call's contents; each
 //     call clears the parts that must start at zero.  Calls that overlap on
-//     the GPU (two streams, two host threads) race on it: serialise them;
+//     the GPU (work still queued on two streams) race on it: serialise them;
+//   - a call holds the library's lock from its set-up to its status read, so
+//     calls from several host threads, and calls beside the library's other
+//     entry points, take turns on the host;
 //   - the first call on a device resolves the array's device address
 //     (cudaGetSymbolAddress) with that device current.  Make that first call
 //     before any stream capture is begun on the device;
-//   - the call reads the kernels' status word back, so it synchronises the
+//   - every call reads the kernels' status word back, so it synchronises the
 //     stream it is given before returning.
 #include "common.cuh"
 
 #include <mutex>
-#include <string>
 
 namespace caps {
 
@@ -44,8 +46,7 @@ constexpr size_t STATUS_OFF = TASK_OFF + 256;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
 constexpr int MAX_DEVICES = 64;
-static void *g_scratch_addr[MAX_DEVICES];
-static std::mutex g_setup_mu;
+static void *g_scratch_addr[MAX_DEVICES];  // guarded by the library lock
 
 __global__ void noalloc_set_task(caps::LeafTask *dst, const double *A, const double *B, double *C) {
     dst->A = A;
@@ -54,7 +55,7 @@ __global__ void noalloc_set_task(caps::LeafTask *dst, const double *A, const dou
 }
 
 // Device address of the scratch array on the current device (set up once per
-// device, with that device current).
+// device, with that device current).  Called with the library lock held.
 caps_status scratch_address(void **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -63,7 +64,6 @@ caps_status scratch_address(void **out) {
         return CAPS_ERR_CUDA;
     }
     if (dev < 0 || dev >= MAX_DEVICES) return CAPS_ERR_UNSUPPORTED;
-    std::lock_guard<std::mutex> g(g_setup_mu);
     if (!g_scratch_addr[dev]) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
@@ -92,6 +92,9 @@ extern "C" caps_status caps_leaf_gemm_split_noalloc_dev(const double *A, const d
         caps::set_last_error_text("split workspace exceeds the no-allocation scratch array");
         return CAPS_ERR_SIZE;
     }
+    // the kernels' per-device set-up (constant tables, attributes) and the
+    // status word are shared with the other entry points
+    std::lock_guard<std::recursive_mutex> lock(caps::library_mutex());
     void *base = nullptr;
     caps_status st = scratch_address(&base);
     if (st != CAPS_OK) return st;

@@ -63,6 +63,12 @@ double getMaxUsedMemory();
 void initCommunication(int *argc, char ***argv, int randomize = 0);
 void initCommunicationAlt(int *argc, char ***argv, int randomize = 0);
 int getRank();
+/* communication.h:12 declares `MPI_Comm getComm()`.  On one rank the value is
+ * MPI_COMM_WORLD of the one-rank MPI stand-in the drivers compile against,
+ * where MPI_Comm is an int (0).  A return type is not part of a C++ symbol
+ * name, so callers built against the reference header link to this one; a
+ * caller whose mpi.h makes MPI_Comm a pointer type must not use the value. */
+int getComm();
 int getLog7nProcs();
 int getPFactor();
 void distributeFrom1Proc(MatDescriptor desc, double *O, double *I);

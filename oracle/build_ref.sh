@@ -6,9 +6,12 @@
 #   oracle/_ref/libcapsref.so                           multiply() & friends
 #   oracle/_ref/libcholref.so                           cholesky/ mult() & friends
 # Usage: oracle/build_ref.sh [REFERENCE_DIR] [THREADS]
+# REFERENCE_DIR defaults to $CAPS_REFERENCE_DIR, then to where this build's
+# container mounts the reference; the directory used is recorded in
+# oracle/_ref/REFERENCE_DIR for the tests that read reference sources.
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-ref="${1:-/root/reference}"
+ref="${1:-${CAPS_REFERENCE_DIR:-/root/reference}}"
 threads="${2:-$(nproc)}"
 out="$here/_ref"
 [ -f "$ref/multiply.cpp" ] || { echo "reference sources not found at $ref" >&2; exit 3; }
@@ -36,4 +39,5 @@ for s in mult.cpp sizes.cpp communication.cpp counters.cpp library.cpp; do
 done
 $CXX -shared -o "$out/libcholref.so" $cobjs $link
 rm -f "$out"/*.o
+echo "$ref" > "$out/REFERENCE_DIR"
 echo "built $out (threads=$threads, blas=$blaslib)"

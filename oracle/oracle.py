@@ -38,6 +38,22 @@ def build(force: bool = False) -> str:
     return LIB
 
 
+def reference_dir():
+    """Directory of the reference sources, or None where they are absent: the
+    CAPS_REFERENCE_DIR environment variable, else the directory
+    build_ref.sh built oracle/_ref from (it records it there)."""
+    cands = [os.environ.get("CAPS_REFERENCE_DIR")]
+    try:
+        with open(os.path.join(HERE, "_ref", "REFERENCE_DIR")) as f:
+            cands.append(f.read().strip())
+    except OSError:
+        pass
+    for c in cands:
+        if c and os.path.isfile(os.path.join(c, "multiply.cpp")):
+            return c
+    return None
+
+
 def openblas_path():
     """Path of numpy's bundled ILP64 OpenBLAS, or None."""
     try:

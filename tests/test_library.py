@@ -9,6 +9,9 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+from oracle.oracle import reference_dir  # noqa: E402
+
+REF = reference_dir() or ""
 
 
 def header_functions(path):
@@ -88,7 +91,7 @@ def test_split_workspace_bounded(caps):
         assert caps.workspace_size(d5, "bbdd", form=form) <= 120000 * 2 ** 20
 
 
-@pytest.mark.skipif(not os.path.isfile("/root/reference/randombenchmark.cpp"), reason="reference sources absent")
+@pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "randombenchmark.cpp")), reason="reference sources absent")
 def test_reference_drivers_link_unmodified_against_library(caps, tmp_path):
     """The reference's own randombenchmark.cpp / fromfile1.cpp compile against
     the reference headers and link against libcaps_gb300.so alone (no
@@ -97,20 +100,21 @@ def test_reference_drivers_link_unmodified_against_library(caps, tmp_path):
     libdir = os.path.dirname(caps.LIB_PATH)
     for drv in ("randombenchmark", "fromfile1"):
         out = tmp_path / drv
-        cmd = ["g++", "-O1", "-w", "-include", shim, "-I" + os.path.dirname(shim), "-I/root/reference",
-               "-DNUM_THREADS=1", "/root/reference/%s.cpp" % drv, "-o", str(out), "-L" + libdir, "-lcaps_gb300",
+        cmd = ["g++", "-O1", "-w", "-include", shim, "-I" + os.path.dirname(shim), "-I" + REF,
+               "-DNUM_THREADS=1", os.path.join(REF, "%s.cpp" % drv), "-o", str(out), "-L" + libdir, "-lcaps_gb300",
                "-Wl,-rpath," + libdir]
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
         assert r.returncode == 0, r.stdout
 
 
-@pytest.mark.skipif(not os.path.isfile("/root/reference/cholesky/test-mult.cpp"), reason="reference sources absent")
+@pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "cholesky", "test-mult.cpp")),
+                    reason="reference sources absent")
 def test_cholesky_test_mult_links_against_library(caps, tmp_path):
     """The Cholesky subproject's own test-mult.cpp, with its sizes /
     communication / counters / library objects but without mult.o, links
     against libcaps_gb300.so: its mult() call resolves to the library's."""
     shim = os.path.join(ROOT, "oracle", "ref_shim")
-    ref = "/root/reference/cholesky"
+    ref = os.path.join(REF, "cholesky")
     libdir = os.path.dirname(caps.LIB_PATH)
     import numpy
     npl = os.path.realpath(os.path.join(os.path.dirname(numpy.__file__), os.pardir, "numpy.libs"))

@@ -8,8 +8,10 @@ import pytest
 
 from helpers import caps_of, mat_of, dd_of
 
+from oracle.oracle import reference_dir
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+REF = reference_dir() or ""
 REFLIB = os.path.join(ROOT, "oracle", "_ref", "libcapsref.so")
 
 
