@@ -43,6 +43,7 @@ C_ABI_SYMBOLS = [
     "caps_get_counters", "caps_reset_counters", "caps_set_phase_timing", "caps_multiply_batched_dev",
     "caps_status_string", "caps_last_cuda_error", "caps_debug_fail_allocations", "caps_release_cache",
     "caps_leaf_gemm_split_noalloc_dev", "caps_autotune_entry", "caps_chol_mult_dev", "caps_chol_mult_host",
+    "caps_debug_starve_split_gemm",
 ]
 
 
@@ -125,6 +126,8 @@ def lib() -> ctypes.CDLL:
         L.caps_last_cuda_error.restype = ctypes.c_char_p
         L.caps_debug_fail_allocations.argtypes = [ctypes.c_int]
         L.caps_debug_fail_allocations.restype = None
+        L.caps_debug_starve_split_gemm.argtypes = [ctypes.c_int]
+        L.caps_debug_starve_split_gemm.restype = None
         L.caps_release_cache.argtypes = []
         L.caps_release_cache.restype = None
         L.caps_leaf_gemm_split_noalloc_dev.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
@@ -329,6 +332,12 @@ def release_cache() -> None:
 
 def debug_fail_allocations(count: int) -> None:
     lib().caps_debug_fail_allocations(int(count))
+
+
+def debug_starve_split_gemm(count: int) -> None:
+    """The next `count` split GEMM launches issue no copies: their bounded
+    waits give up and the call raises CapsError(CAPS_ERR_TIMEOUT)."""
+    lib().caps_debug_starve_split_gemm(int(count))
 
 
 @dataclass

@@ -137,12 +137,17 @@ void split_gemm_prepare();
 cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, SplitParams p,
                               void *workspace, unsigned int *status_dev, cudaStream_t stream);
 
+// Test hook behind caps_debug_starve_split_gemm: the next `count` split GEMM
+// launches issue no copies, so their first bounded waits give up (with a
+// short limit: nothing is in flight) and the call returns CAPS_ERR_TIMEOUT.
+void set_debug_starve(int count);
+
 // kernels_crt.cu, called by the launchers above
 cudaError_t crt_prepare();
 cudaError_t launch_crt_resolve(int count, int m, SplitParams p, void *workspace, cudaStream_t stream);
 cudaError_t launch_crt_slice(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
                              cudaStream_t stream);
 cudaError_t launch_crt_gemm(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
-                            unsigned int *status_dev, int num_sms, cudaStream_t stream);
+                            unsigned int *status_dev, int num_sms, cudaStream_t stream, int starve = 0);
 
 }  // namespace caps

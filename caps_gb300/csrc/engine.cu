@@ -1383,6 +1383,11 @@ caps_status caps_autotune_entry(int index, int *n, int *form, int *nrec, char *p
 
 void caps_debug_fail_allocations(int count) { g_fail_allocs = count > 0 ? count : 0; }
 
+void caps_debug_starve_split_gemm(int count) {
+    std::lock_guard<std::recursive_mutex> g(g_mu);
+    set_debug_starve(count);
+}
+
 void caps_release_cache(void) {
     std::lock_guard<std::recursive_mutex> g(g_mu);
     cudaDeviceSynchronize();

@@ -483,10 +483,13 @@ __device__ __forceinline__ void crt_reconstruct4(const uint32_t (&zq)[LMAX], int
 // of one modulus of about one leaf (16 MB at m = 2048) through L2.
 __global__ void __launch_bounds__(RGEMM_THREADS, 1)
     crt_gemm_kernel(const LeafTask *__restrict__ tasks, char *__restrict__ ws, Geo g,
-                    unsigned *__restrict__ status) {
+                    unsigned *__restrict__ status, int starve) {
     const SplitHdr *h = reinterpret_cast<const SplitHdr *>(ws);
     if (!h->residues) return;  // the digit scheme runs
     const int L = h->moduli;
+    // starve (test hook): no copies are issued, so nothing is ever in flight
+    // and every wait may give up after a short spin
+    const uint32_t wl = starve ? WAIT_LIMIT_STARVED : WAIT_LIMIT;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     unsigned char *stA = smem;                        // RNSTAGE x RSTAGE_A
@@ -538,7 +541,7 @@ __global__ void __launch_bounds__(RGEMM_THREADS, 1)
             uint32_t phase = 0;
             bool ok = true;
             uint32_t armed[RNSTAGE] = {0, 0, 0, 0};  // 1 + phase of the last arm
-            for (int64_t u = blockIdx.x; u < total && ok; u += gridDim.x) {
+            for (int64_t u = blockIdx.x; u < total && ok && !starve; u += gridDim.x) {
                 const int leafi = (int)(u / tiles);
                 const int64_t tile = u % tiles;
                 const int mt = (int)(tile / g.rtiles), rt = (int)(tile % g.rtiles);
@@ -548,7 +551,7 @@ __global__ void __launch_bounds__(RGEMM_THREADS, 1)
                     const char *srcB = pl + g.off_rb + (((size_t)l * g.rtiles + rt) * nks) * RB_TILE;
                     for (int ks = 0; ks < nks; ks += RSTAGE_K) {
                         const uint32_t n = ks + RSTAGE_K <= nks ? RSTAGE_K : (uint32_t)(nks - ks);
-                        if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, status, RSTATUS << 0)) { ok = false; break; }
+                        if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, status, RSTATUS << 0, wl)) { ok = false; break; }
                         mbar_expect_tx(full0 + 8 * stage, n * (RA_TILE + RB_TILE));
                         bulk_g2s(smem_u32(stA + stage * RSTAGE_A), srcA + (size_t)ks * RA_TILE, n * RA_TILE,
                                  full0 + 8 * stage);
@@ -561,7 +564,7 @@ __global__ void __launch_bounds__(RGEMM_THREADS, 1)
             }
             // every armed stage's copies land before the CTA exits
             for (int i = 0; i < RNSTAGE; i++)
-                if (armed[i]) mbar_wait(full0 + 8 * i, armed[i] - 1, status, RSTATUS << 1);
+                if (armed[i]) mbar_wait(full0 + 8 * i, armed[i] - 1, status, RSTATUS << 1, wl);
         }
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
@@ -575,12 +578,12 @@ __global__ void __launch_bounds__(RGEMM_THREADS, 1)
             for (int64_t u = blockIdx.x; u < total && ok; u += gridDim.x) {
                 for (int l = 0; l < L && ok; l++, uc++) {
                     const uint32_t acc = uc & 1;
-                    if (!mbar_wait(tempty0 + 8 * acc, ((uc >> 1) & 1) ^ 1, status, RSTATUS << 2)) { ok = false; break; }
+                    if (!mbar_wait(tempty0 + 8 * acc, ((uc >> 1) & 1) ^ 1, status, RSTATUS << 2, wl)) { ok = false; break; }
                     tc_fence_after();
                     const uint32_t dt = tmem + acc * RTN;
                     for (int ks = 0; ks < nks; ks += RSTAGE_K) {
                         const int n = ks + RSTAGE_K <= nks ? RSTAGE_K : nks - ks;
-                        if (!mbar_wait(full0 + 8 * stage, phase, status, RSTATUS << 3)) { ok = false; break; }
+                        if (!mbar_wait(full0 + 8 * stage, phase, status, RSTATUS << 3, wl)) { ok = false; break; }
                         tc_fence_after();
                         const uint64_t sa = (uint64_t)((uint32_t)stage * RSTAGE_A) >> 4;
                         const uint64_t sb = (uint64_t)((uint32_t)stage * RSTAGE_B) >> 4;
@@ -598,7 +601,7 @@ __global__ void __launch_bounds__(RGEMM_THREADS, 1)
             }
             // every issued MMA completes before TMEM is released
             umma_commit(finalb);
-            mbar_wait(finalb, 0, status, RSTATUS << 4);
+            mbar_wait(finalb, 0, status, RSTATUS << 4, wl);
         }
     } else if (warp < 10) {
         // ------------------------------------------------ drain (8 warps)
@@ -610,13 +613,13 @@ __global__ void __launch_bounds__(RGEMM_THREADS, 1)
         for (int64_t u = blockIdx.x; u < total && ok; u += gridDim.x, tc++) {
             const uint32_t zb = tc & 1;
             // the reconstruction warps are done with this residue tile
-            const bool free_ = mbar_wait(zempty0 + 8 * zb, ((tc >> 1) & 1) ^ 1, status, RSTATUS << 6);
+            const bool free_ = mbar_wait(zempty0 + 8 * zb, ((tc >> 1) & 1) ^ 1, status, RSTATUS << 6, wl);
             if (!__all_sync(0xffffffffu, free_)) break;
             unsigned char *zt = ztiles + (size_t)zb * ZTILE_BYTES + row;
             for (int l = 0; l < L; l++, uc++) {
                 const uint32_t acc = uc & 1;
                 // warp-uniform: tcgen05.ld below is .sync.aligned
-                const bool got = mbar_wait(tfull0 + 8 * acc, (uc >> 1) & 1, status, RSTATUS << 5);
+                const bool got = mbar_wait(tfull0 + 8 * acc, (uc >> 1) & 1, status, RSTATUS << 5, wl);
                 if (!__all_sync(0xffffffffu, got)) { ok = false; break; }
                 tc_fence_after();
                 const float p = c_crt.p[l], invp = c_crt.invp[l];
@@ -656,7 +659,7 @@ __global__ void __launch_bounds__(RGEMM_THREADS, 1)
         uint32_t tc = 0;
         for (int64_t u = blockIdx.x; u < total; u += gridDim.x, tc++) {
             const uint32_t zb = tc & 1;
-            const bool got = mbar_wait(zfull0 + 8 * zb, (tc >> 1) & 1, status, RSTATUS << 7);
+            const bool got = mbar_wait(zfull0 + 8 * zb, (tc >> 1) & 1, status, RSTATUS << 7, wl);
             if (!__all_sync(0xffffffffu, got)) break;
             const int leafi = (int)(u / tiles);
             const int64_t tile = u % tiles;
@@ -770,7 +773,7 @@ cudaError_t launch_crt_slice(const LeafTask *tasks_dev, int count, int m, SplitP
 }
 
 cudaError_t launch_crt_gemm(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
-                            unsigned int *status_dev, int num_sms, cudaStream_t stream) {
+                            unsigned int *status_dev, int num_sms, cudaStream_t stream, int starve) {
     Geo g = make_geo(m, count, p.scheme);
     if (!g.residues_ok) return cudaSuccess;
     cudaError_t e = crt_prepare();
@@ -779,7 +782,7 @@ cudaError_t launch_crt_gemm(const LeafTask *tasks_dev, int count, int m, SplitPa
     int grid = (int)(units < num_sms ? units : num_sms);
     if (grid > ZCTA_MAX) grid = ZCTA_MAX;  // two product-residue tiles per CTA
     const size_t smem = (size_t)RNSTAGE * RSTAGE_BYTES + 1024 + 1024;
-    crt_gemm_kernel<<<grid, RGEMM_THREADS, smem, stream>>>(tasks_dev, (char *)workspace, g, status_dev);
+    crt_gemm_kernel<<<grid, RGEMM_THREADS, smem, stream>>>(tasks_dev, (char *)workspace, g, status_dev, starve);
     count_launch();
     return cudaGetLastError();
 }

@@ -359,7 +359,7 @@ __device__ void build_mma_table(MmaTable *t, uint32_t a0, uint32_t b0, int s, in
 
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     split_gemm_kernel(const LeafTask *__restrict__ tasks, int count, char *__restrict__ ws, Geo g,
-                      SplitParams p, unsigned *__restrict__ status) {
+                      SplitParams p, unsigned *__restrict__ status, int starve) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     unsigned char *stA = smem;                      // NSTAGE x STAGE_A
@@ -371,6 +371,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 
     if (reinterpret_cast<const SplitHdr *>(ws)->residues) return;  // the residue scheme runs
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // starve (test hook): no copies are issued, so nothing is ever in flight
+    // and every wait may give up after a short spin
+    const uint32_t wl = starve ? WAIT_LIMIT_STARVED : WAIT_LIMIT;
     int s, nd;
     resolve_sd(reinterpret_cast<const SplitHdr *>(ws), p, s, nd);
     const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + NSTAGE);
@@ -411,7 +414,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             uint32_t phase = 0;
             bool ok = true;
             uint32_t armed[NSTAGE] = {0, 0};  // 1 + phase of the last arm
-            for (int64_t tile = blockIdx.x; tile < total && ok; tile += gridDim.x) {
+            for (int64_t tile = blockIdx.x; tile < total && ok && !starve; tile += gridDim.x) {
                 int leafi = (int)(tile / tiles_per_leaf);
                 int64_t rem = tile % tiles_per_leaf;
                 int mt = (int)(rem / g.ntiles), nt = (int)(rem % g.ntiles);
@@ -423,7 +426,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                     for (int ks = ks0; ks < ks1; ks += SUB) {
                         // SUB consecutive 16-deep tiles are adjacent in global memory
                         const uint32_t nsub = ks + SUB <= ks1 ? SUB : (uint32_t)(ks1 - ks);
-                        if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, status, 1u)) { ok = false; break; }
+                        if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, status, 1u, wl)) { ok = false; break; }
                         mbar_expect_tx(full0 + 8 * stage, nsub * (bytesA + bytesB));
                         bulk_g2s(smem_u32(stA + stage * STAGE_A), srcA + (size_t)ks * bytesA, nsub * bytesA,
                                  full0 + 8 * stage);
@@ -436,7 +439,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             }
             // drain: every armed stage's copies must land before exit
             for (int i = 0; i < NSTAGE; i++)
-                if (armed[i]) mbar_wait(full0 + 8 * i, armed[i] - 1, status, 2u);
+                if (armed[i]) mbar_wait(full0 + 8 * i, armed[i] - 1, status, 2u, wl);
         }
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
@@ -458,12 +461,12 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             bool ok = true;
             for (int64_t tile = blockIdx.x; tile < total && ok; tile += gridDim.x) {
                 for (int ch = 0; ch < nchunks && ok; ch++) {
-                    if (!mbar_wait(tempty, (chunk_ctr & 1) ^ 1, status, 4u)) { ok = false; break; }
+                    if (!mbar_wait(tempty, (chunk_ctr & 1) ^ 1, status, 4u, wl)) { ok = false; break; }
                     tc_fence_after();
                     int ks0 = ch * CHUNK, ks1 = ks0 + CHUNK < g.nks ? ks0 + CHUNK : g.nks;
                     for (int ks = ks0; ks < ks1; ks += SUB) {
                         const int nsub = ks + SUB <= ks1 ? SUB : ks1 - ks;
-                        if (!mbar_wait(full0 + 8 * stage, phase, status, 8u)) { ok = false; break; }
+                        if (!mbar_wait(full0 + 8 * stage, phase, status, 8u, wl)) { ok = false; break; }
                         tc_fence_after();
 #pragma unroll
                         for (int sub = 0; sub < SUB; sub++) {
@@ -486,7 +489,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             }
             // all issued MMAs complete before TMEM is released
             umma_commit(finalb);
-            mbar_wait(finalb, 0, status, 16u);
+            mbar_wait(finalb, 0, status, 16u, wl);
         }
     } else {
         // ------------------------------------------------ epilogue (8 warps)
@@ -503,7 +506,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             for (int c = 0; c < 32; c++) hi[c] = lo[c] = 0;
             for (int ch = 0; ch < nchunks; ch++) {
                 // warp-uniform: tcgen05.ld below is .sync.aligned
-                bool got = mbar_wait(tfull, chunk_ctr & 1, status, 32u);
+                bool got = mbar_wait(tfull, chunk_ctr & 1, status, 32u, wl);
                 if (!__all_sync(0xffffffffu, got)) { ok = false; break; }
                 tc_fence_after();
                 for (int r = 0; r < nd; r++) {
@@ -618,8 +621,15 @@ cudaError_t launch_split_prep(const LeafTask *tasks_dev, int count, int m, Split
     return cudaGetLastError();
 }
 
+static int g_debug_starve = 0;
+void set_debug_starve(int count) { g_debug_starve = count > 0 ? count : 0; }
+
 cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
                               unsigned int *status_dev, cudaStream_t stream) {
+    // one starved call covers both GEMM launches (the one for the scheme not
+    // chosen returns at once)
+    const int starve = g_debug_starve > 0 ? 1 : 0;
+    if (starve) g_debug_starve--;
     Geo g = make_geo(m, count, p.scheme);
     char *ws = (char *)workspace;
     cudaError_t e;
@@ -630,12 +640,12 @@ cudaError_t launch_split_gemm(const LeafTask *tasks_dev, int count, int m, Split
     if (!(p.scheme == SCHEME_RESIDUES && g.residues_ok)) {  // see launch_split_prep
         int64_t total = (int64_t)g.mtiles * g.ntiles * count;
         int grid = (int)(total < g_num_sms ? total : g_num_sms);
-        split_gemm_kernel<<<grid, GEMM_THREADS, smem, stream>>>(tasks_dev, count, ws, g, p, status_dev);
+        split_gemm_kernel<<<grid, GEMM_THREADS, smem, stream>>>(tasks_dev, count, ws, g, p, status_dev, starve);
         count_launch();
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    return launch_crt_gemm(tasks_dev, count, m, p, ws, status_dev, g_num_sms, stream);
+    return launch_crt_gemm(tasks_dev, count, m, p, ws, status_dev, g_num_sms, stream, starve);
 }
 
 }  // namespace caps

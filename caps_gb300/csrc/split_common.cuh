@@ -18,6 +18,9 @@ constexpr int RKMAX = 2048;    // residue scheme: max K (K * 90^2 < 2^24: exact 
 constexpr int ZCTA_MAX = 160;  // residue scheme: GEMM CTAs with product-residue scratch
 constexpr size_t ZTILE_BYTES = (size_t)LMAX * TM * RTN;  // product residues of one tile
 constexpr uint32_t WAIT_LIMIT = 1u << 25;
+// wait limit of a GEMM launch the starvation test hook runs: it issues no
+// copies, so its waits have nothing in flight and may give up early
+constexpr uint32_t WAIT_LIMIT_STARVED = 1u << 12;
 
 enum { SCHEME_AUTO = 0, SCHEME_DIGITS = 1, SCHEME_RESIDUES = 2 };
 
@@ -184,8 +187,8 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
 
 // bounded wait: false (and a status bit) if the phase never completes
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned *status,
-                                          unsigned code) {
-    for (uint32_t it = 0; it < WAIT_LIMIT; it++) {
+                                          unsigned code, uint32_t limit = WAIT_LIMIT) {
+    for (uint32_t it = 0; it < limit; it++) {
         if (mbar_try(bar, parity)) return true;
         if (it > 64) __nanosleep(it > 4096 ? 256 : 32);
     }

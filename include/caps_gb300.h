@@ -208,6 +208,13 @@ const char *caps_last_cuda_error(void);
  * injection, no GPU fault).  count <= 0 disables. */
 void caps_debug_fail_allocations(int count);
 
+/* Test hook for the bounded device waits: the next `count` split-form GEMM
+ * launches issue no copies, so their waits have nothing in flight and give up
+ * after a short spin; the call returns CAPS_ERR_TIMEOUT, with TMEM freed and
+ * the context usable, and the next call runs normally.  No fault, trap or
+ * hang is involved.  count <= 0 disables. */
+void caps_debug_starve_split_gemm(int count);
+
 /* Releases cached workspace and plans. */
 void caps_release_cache(void);
 

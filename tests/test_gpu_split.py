@@ -235,3 +235,30 @@ def test_residue_scheme_falls_back_to_digits_above_2048(caps, oracle_mod, cuda):
     Cd, cnt_d = _leaf(caps, cuda, A, B, scheme="digits")
     assert cnt_r["split_moduli"] == 0 and cnt_r["split_slices"] == 8
     assert np.array_equal(Cr, Cd)
+
+
+@pytest.mark.parametrize("scheme", ["residues", "digits"])
+def test_starved_gemm_wait_gives_up_then_next_call_runs(caps, oracle_mod, cuda, scheme):
+    """The bounded device waits: a GEMM launch that is given no copies (test
+    hook; nothing is in flight, no fault) gives up its waits, frees TMEM and
+    returns CAPS_ERR_TIMEOUT; the context stays usable and the next call is
+    exact against the oracle's model."""
+    import time
+    m = 256
+    rng = np.random.default_rng(77)
+    A = rng.uniform(-1, 1, (m, m))
+    B = rng.uniform(-1, 1, (m, m))
+    caps.debug_starve_split_gemm(1)
+    t0 = time.perf_counter()
+    with pytest.raises(caps.CapsError) as e:
+        _leaf(caps, cuda, A, B, scheme=scheme)
+    waited = time.perf_counter() - t0
+    assert e.value.status == 6, e.value
+    assert waited < 30.0
+    C, cnt = _leaf(caps, cuda, A, B, scheme=scheme)
+    if scheme == "residues":
+        ref, _ = oracle_mod.split_gemm_residues(A.T.copy().reshape(-1), B.T.copy().reshape(-1), m)
+    else:
+        ref = oracle_mod.split_gemm(A.T.copy().reshape(-1), B.T.copy().reshape(-1), m, cnt["split_slices"],
+                                    cnt["split_diagonals"])
+    assert np.array_equal(C, ref.reshape(m, m).T)
