@@ -17,7 +17,7 @@ classical product.
             its tensor flops per launch / its average launch time (CUDA events,
             same stream)
   cpu_baseline  the oracle restatement of the reference's CPU path (OpenMP +
-            OpenBLAS dgemm) on a bounded sample of the same workload
+            OpenBLAS dgemm): one whole multiply of the same workload, timed
 
 --impl reference times the reference's CPU path alone (the oracle port on the
 host cores), as the reference arm.  N > 1 GPUs (torchrun) run independent
@@ -221,10 +221,10 @@ def sampled_error(C_cm, A_cm, B_cm, n, samples, seed=7):
 
 
 # ----------------------------------------------------------------- CPU leg
-def cpu_sample(n, nrec, seed=11):
-    """Oracle port of the reference CPU path on a bounded sample of the
-    workload: the top level's sums and C combination in full plus one of its
-    seven subproducts (n/2, nrec-1) in full; t_full ~ t_top + 7 t_sub."""
+def cpu_setup(n, seed=11):
+    """Threads, OpenBLAS leaves and seeded uniform[-1,1) inputs for the oracle
+    port of the reference CPU path (randombenchmark.cpp:19-22 draws the same
+    distribution)."""
     import numpy as np
     from oracle import oracle
     cores = os.cpu_count() or 1
@@ -234,41 +234,61 @@ def cpu_sample(n, nrec, seed=11):
     rng = np.random.default_rng(seed)
     A = rng.uniform(-1, 1, n * n)
     B = rng.uniform(-1, 1, n * n)
+    return oracle, A, B, cores, blas
+
+
+def cpu_whole_multiplies(n, nrec, count, seed=11):
+    """Seconds of each of `count` whole n x n, nrec-level 'd'*nrec multiplies
+    of the oracle port of the reference CPU path (OpenMP sums, OpenBLAS dgemm
+    leaves), timed as randombenchmark.cpp:89-93 times multiply(): a timer
+    read on each side of the call.  One rank runs 'd' steps: a 'b' step
+    needs more than one rank."""
+    oracle, A, B, cores, blas = cpu_setup(n, seed)
+    times = []
+    for _ in range(count):
+        t0 = time.perf_counter()
+        oracle.multiply(A, B, n, nrec, 1, "d" * nrec)
+        times.append(time.perf_counter() - t0)
+    return times, cores, blas
+
+
+def cpu_sample_model(n, nrec, seed=11):
+    """Cross-check only: the top level's sums and C combination timed in full
+    plus one of its seven subproducts (n/2, nrec-1) timed in full; a whole
+    multiply takes about t_top + 7 t_sub."""
+    import numpy as np
+    oracle, A, B, cores, blas = cpu_setup(n, seed)
     C = np.empty(n * n)
     t_top, t_sub = oracle.multiply_sample(A, B, C, n, nrec, 1, "d" * nrec, child=1)
-    t_full = t_top + 7 * t_sub
-    del A, B, C
-    return {"t_top": t_top, "t_sub": t_sub, "t_est": t_full, "cores": cores, "blas": blas}
+    return {"t_top_s": t_top, "t_sub_s": t_sub, "t_model_s": t_top + 7 * t_sub,
+            "model": "t_top + 7 t_sub (top-level sums and combination + one of seven subproducts)"}
 
 
-def cpu_baseline_entry(n, nrec, s):
-    return {"value": 2.0 * n ** 3 / s["t_est"] / 1e12, "unit": "TFLOP/s", "cores": s["cores"], "kind": "port",
-            "sample": "oracle restatement of the reference CPU path (OpenMP sums, OpenBLAS dgemm leaves, "
-                      "OMP_WAIT_POLICY=passive, %d threads): n=%d r=%d 'd'*r, top-level sums and C combination "
-                      "timed in full (%.2f s) plus 1 of the 7 top-level subproducts (n=%d, r=%d) timed in full "
-                      "(%.2f s); value = 2n^3 / (t_top + 7 t_sub)" % (s["cores"], n, nrec, s["t_top"], n // 2,
-                                                                     nrec - 1, s["t_sub"])}
+def cpu_sample_text(n, nrec, count, cores, blas):
+    return ("oracle restatement of the reference CPU path (OpenMP sums, %s dgemm leaves, OMP_WAIT_POLICY=passive, "
+            "%d threads): %d whole multiplies n=%d r=%d pattern '%s', each timed around the call"
+            % ("OpenBLAS" if blas else "loop", cores, count, n, nrec, "d" * nrec))
 
 
 def run_reference(args, world, rank):
     if rank != 0:
         return
     n, r = args.n, args.nrec
-    times = []
-    for k in range(args.warmup + args.steps):
-        s = cpu_sample(n, r, seed=11 + k)
-        if k >= args.warmup:
-            times.append(s)
-    t = sum(x["t_est"] for x in times) / len(times)
+    times, cores, blas = cpu_whole_multiplies(n, r, args.warmup + args.steps)
+    timed = times[args.warmup:]
+    model = cpu_sample_model(n, r)  # cross-check of the earlier sampled estimate
+    t = sum(timed) / len(timed)
     val = 2.0 * n ** 3 / t / 1e12
-    cb = cpu_baseline_entry(n, r, {**times[-1], "t_est": t})
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": val, "unit": "TFLOP/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "CAPS Strassen multiply n=%d r=%d, reference CPU path (one rank)" % (n, r),
                    "n": n, "nrec": r, "pattern": "d" * r, "inputs": "uniform[-1,1) seeded"},
-        "cpu_baseline": cb,
+        "step_ms": [x * 1e3 for x in timed], "warmup_ms": [x * 1e3 for x in times[:args.warmup]],
+        "sample_model": model,
+        "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                         "sample": cpu_sample_text(n, r, len(timed), cores, blas)},
         "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
@@ -655,12 +675,27 @@ def main():
     e2e_pattern = cg.resolve_pattern(desc, None, form="split", workspace_limit=96 << 30)
     cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices, scheme=args.scheme)
     barrier(world)
+    e2e_steps = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
+        ts = time.perf_counter()
         cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices, scheme=args.scheme)
+        e2e_steps.append((time.perf_counter() - ts) * 1e3)
     t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
     # the copy rates again: on a shared host they can drop while the leg runs
     copy_bw_after = pinned_copy_bandwidth(hA, A, stream)
+    # one more call with timing events on the copy stream: where its time goes
+    cg.set_phase_timing(True)
+    ts = time.perf_counter()
+    cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices, scheme=args.scheme)
+    tl_wall = (time.perf_counter() - ts) * 1e3
+    cg.set_phase_timing(False)
+    tc = cg.counters()
+    e2e_timeline = {"wall_ms": tl_wall, "first_inputs_ms": tc["host_first_inputs"] * 1e3,
+                    "all_inputs_ms": tc["host_all_inputs"] * 1e3, "compute_end_ms": tc["host_compute_end"] * 1e3,
+                    "copy_back_end_ms": tc["host_copy_back_end"] * 1e3,
+                    "meaning": "device times from the call's start: A11+B11 on the device, all inputs on the "
+                               "device, last kernel done, last C quadrant on the host"}
     barrier(world)
 
     # ---- plain FP64 Strassen of the same multiply, and the errors of both
@@ -729,7 +764,9 @@ def main():
         cpu = None
         if not args.no_cpu:
             try:
-                cpu = cpu_baseline_entry(n, r, cpu_sample(n, r))
+                times, cores, blas = cpu_whole_multiplies(n, r, 1)
+                cpu = {"value": 2.0 * n ** 3 / times[0] / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                       "sample": cpu_sample_text(n, r, 1, cores, blas), "seconds": times[0]}
             except Exception as ex:  # the baseline is reported, never required
                 cpu = {"value": None, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
                        "sample": "failed: %s" % ex}
@@ -761,7 +798,8 @@ def main():
             "cpu_baseline": cpu,
             "e2e": {"value": world * 2.0 * n ** 3 / t_e2e / 1e12, "unit": "TFLOP/s",
                     "h2d_bytes_per_step": 2 * n * n * 8, "d2h_bytes_per_step": n * n * 8,
-                    "ms_per_step": t_e2e * 1e3, "pinned_copy_gbs": copy_bw,
+                    "ms_per_step": t_e2e * 1e3, "step_ms": e2e_steps, "timeline": e2e_timeline,
+                    "pinned_copy_gbs": copy_bw,
                     "pinned_copy_gbs_after_e2e": copy_bw_after,
                     "pinned_copy_gbs_after_error_checks": out.get("copy_bw_late"),
                     "api": "caps_multiply_host, pinned host buffers, no pattern given: top level 'd' + %s "

@@ -79,7 +79,9 @@ class Counters(ctypes.Structure):
                 ("split_slices", ctypes.c_int), ("split_diagonals", ctypes.c_int),
                 ("kernel_launches", ctypes.c_longlong), ("time_leaf_gemm", ctypes.c_double),
                 ("leaf_gemm_launches", ctypes.c_longlong), ("leaf_gemm_m3", ctypes.c_double),
-                ("add_bytes", ctypes.c_longlong), ("split_moduli", ctypes.c_int), ("split_pad", ctypes.c_int)]
+                ("add_bytes", ctypes.c_longlong), ("split_moduli", ctypes.c_int), ("split_pad", ctypes.c_int),
+                ("host_first_inputs", ctypes.c_double), ("host_all_inputs", ctypes.c_double),
+                ("host_compute_end", ctypes.c_double), ("host_copy_back_end", ctypes.c_double)]
 
 
 _lib = None

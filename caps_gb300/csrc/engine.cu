@@ -590,6 +590,8 @@ struct HostSide {
     cudaEvent_t start = nullptr;             // earlier work on the caller's stream is done
     cudaEvent_t c_ready = nullptr;           // caps_chol_mult_host: C is on the device
     cudaEvent_t events[HOST_EVENTS] = {};    // caps_multiply_host: quadrant hand-offs
+    cudaEvent_t timing[5] = {};              // phase timing: start, first inputs, all inputs,
+                                             // compute end, copy-back end
 };
 static std::deque<HostSide> g_host_sides;  // deque: elements stay put as devices are added
 
@@ -607,6 +609,7 @@ static caps_status host_side(HostSide **out) {
     CAPS_CUDA_TRY(cudaEventCreateWithFlags(&h.start, cudaEventDisableTiming));
     CAPS_CUDA_TRY(cudaEventCreateWithFlags(&h.c_ready, cudaEventDisableTiming));
     for (int i = 0; i < HOST_EVENTS; i++) CAPS_CUDA_TRY(cudaEventCreateWithFlags(&h.events[i], cudaEventDisableTiming));
+    for (int i = 0; i < 5; i++) CAPS_CUDA_TRY(cudaEventCreate(&h.timing[i]));
     g_host_sides.push_back(h);
     *out = &g_host_sides.back();
     return CAPS_OK;
@@ -1166,13 +1169,18 @@ caps_status caps_multiply_host(const double *A, const double *B, double *C, caps
     auto h2d = [&](double *dst, const double *src, int quad) {
         return cudaMemcpyAsync((char *)dst + quad * q, (const char *)src + quad * q, q, cudaMemcpyHostToDevice, cs);
     };
+    const bool timeline = g_phase_timing;  // where the call's time goes (timing events)
+    g_counters.host_first_inputs = g_counters.host_all_inputs = 0;
+    g_counters.host_compute_end = g_counters.host_copy_back_end = 0;
     CAPS_CUDA_TRY(cudaEventRecord(start, s));  // after earlier work on s
     CAPS_CUDA_TRY(cudaStreamWaitEvent(cs, start, 0));
+    if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[0], cs));
     // quadrants X11, X21, X12, X22 at 0, q, 2q, 3q: A11 + B11 (Q1), then
     // A12 + B21 (Q2), then the rest
     CAPS_CUDA_TRY(h2d(dA, A, 0));
     CAPS_CUDA_TRY(h2d(dB, B, 0));
     CAPS_CUDA_TRY(cudaEventRecord(g_host_events[0], cs));
+    if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[1], cs));
     CAPS_CUDA_TRY(h2d(dA, A, 2));
     CAPS_CUDA_TRY(h2d(dB, B, 1));
     CAPS_CUDA_TRY(cudaEventRecord(g_host_events[1], cs));
@@ -1181,11 +1189,17 @@ caps_status caps_multiply_host(const double *A, const double *B, double *C, caps
     CAPS_CUDA_TRY(h2d(dB, B, 2));
     CAPS_CUDA_TRY(h2d(dB, B, 3));
     CAPS_CUDA_TRY(cudaEventRecord(g_host_events[2], cs));
+    if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[2], cs));
+    // the plan's own phase timing would synchronise inside the call and
+    // serialise the copies back behind the whole multiply: off here
+    g_phase_timing = false;
     caps_status st = multiply_dev_locked(dA, dB, dC, desc, pat, o, s, false, true);
+    g_phase_timing = timeline;
     if (st != CAPS_OK) {
         cudaStreamSynchronize(cs);
         return st;
     }
+    if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[3], s));
     // C11 (quadrant 0), C22 (3), C21 (1), C12 (2) as they become final
     const int quad_of_event[HOST_EVENTS - EV_C_FIRST] = {0, 3, 1, 2};
     for (int e = EV_C_FIRST; e < HOST_EVENTS; e++) {
@@ -1193,9 +1207,19 @@ caps_status caps_multiply_host(const double *A, const double *B, double *C, caps
         const int quad = quad_of_event[e - EV_C_FIRST];
         CAPS_CUDA_TRY(cudaMemcpyAsync((char *)C + quad * q, (char *)dC + quad * q, q, cudaMemcpyDeviceToHost, cs));
     }
+    if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[4], cs));
     if (o.form == CAPS_FORM_SPLIT) CAPS_TRY(check_device_status(s, nullptr));
     CAPS_CUDA_TRY(cudaStreamSynchronize(s));
     CAPS_CUDA_TRY(cudaStreamSynchronize(cs));
+    if (timeline) {
+        double *out[4] = {&g_counters.host_first_inputs, &g_counters.host_all_inputs, &g_counters.host_compute_end,
+                          &g_counters.host_copy_back_end};
+        for (int i = 0; i < 4; i++) {
+            float ms = 0;
+            CAPS_CUDA_TRY(cudaEventElapsedTime(&ms, hs->timing[0], hs->timing[i + 1]));
+            *out[i] = ms * 1e-3;
+        }
+    }
     return CAPS_OK;
 }
 
@@ -1409,6 +1433,7 @@ void caps_release_cache(void) {
         cudaEventDestroy(h.start);
         cudaEventDestroy(h.c_ready);
         for (int i = 0; i < HOST_EVENTS; i++) cudaEventDestroy(h.events[i]);
+        for (int i = 0; i < 5; i++) cudaEventDestroy(h.timing[i]);
     }
     g_host_sides.clear();
     g_host_events = nullptr;

@@ -175,6 +175,14 @@ typedef struct caps_counters {
     long long add_bytes;     /* algorithmic bytes read + written by the sum / combination kernels */
     int split_moduli;        /* moduli used by the last split multiply's residue scheme (0: digits ran) */
     int split_pad;
+    /* caps_multiply_host with phase timing on: seconds from the call's start
+     * on the device to the first input quadrants (A11, B11) being on the
+     * device, to all inputs being on the device, to the last kernel, and to
+     * the last C quadrant being back on the host (0 otherwise) */
+    double host_first_inputs;
+    double host_all_inputs;
+    double host_compute_end;
+    double host_copy_back_end;
 } caps_counters;
 
 void caps_get_counters(caps_counters *out);
