@@ -754,6 +754,10 @@ cudaError_t crt_prepare() {
 }
 
 cudaError_t launch_crt_resolve(int count, int m, SplitParams p, void *workspace, cudaStream_t stream) {
+    // the resolve reads the moduli tables: they must be on the device before
+    // the first launch group of the process (returns at once afterwards)
+    cudaError_t e = crt_prepare();
+    if (e != cudaSuccess) return e;
     Geo g = make_geo(m, count, p.scheme);
     crt_resolve_kernel<<<1, 32, 0, stream>>>((char *)workspace, g, p);
     count_launch();

@@ -71,7 +71,7 @@ size_t split_workspace_bytes(int m, int count, int scheme) {
 constexpr int SCAN_AROWS = 512, SCAN_KSLAB = 128, SCAN_BCOLS = 32;
 
 __device__ __forceinline__ void scan_value(double x, int &emax, int &lmin) {
-    if ((unsigned long long)__double_as_longlong(x) << 1) {  // x != 0 by its encoding (an FP64 compare runs at 1/64 rate)
+    if (nonzero_bits(x)) {
         int E, lb;
         exp_lsb(x, E, lb);
         emax = E > emax ? E : emax;
