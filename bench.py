@@ -643,6 +643,7 @@ def main():
     torch.cuda.synchronize()
     cg.set_phase_timing(True)
     gemm_t, gemm_launches, gemm_m3, launches = 0.0, 0, 0.0, 0
+    add_t, add_b = 0.0, 0
     barrier(world)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -655,12 +656,39 @@ def main():
             gemm_launches += c["leaf_gemm_launches"]
             gemm_m3 += c["leaf_gemm_m3"]
             launches += c["kernel_launches"]
+            add_t += c["time_add"]
+            add_b += c["add_bytes"]
         e1.record(stream)
         torch.cuda.synchronize()
     barrier(world)
     cg.set_phase_timing(False)
     t_split = max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps, world)
     cnt = cg.counters()
+    peaks0, _ = measured_peaks()
+    hbm_peak = float(peaks0.get("hbm_gbs", 6800.0))
+    # the layout reorder (communication.cpp:612-704) both ways on the same
+    # matrices: 16 bytes moved per element, CUDA events on the stream
+    tmp, back = torch.empty_like(A), torch.empty_like(A)
+    cg.from_caps_layout(A, tmp, desc, stream=stream.cuda_stream)
+    r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    r0.record(stream)
+    for _ in range(3):
+        cg.from_caps_layout(A, tmp, desc, stream=stream.cuda_stream)
+        cg.to_caps_layout(tmp, back, desc, stream=stream.cuda_stream)
+    r1.record(stream)
+    torch.cuda.synchronize()
+    reorder_gbs = 6 * 16.0 * n * n / (r0.elapsed_time(r1) / 1e3) / 1e9
+    reorder_roundtrip_exact = bool(torch.equal(back, A))
+    del tmp, back
+    memory_kernels = {
+        "reorder": {"gbs": reorder_gbs, "frac_of_hbm_copy": reorder_gbs / hbm_peak,
+                    "round_trip_exact": reorder_roundtrip_exact,
+                    "bytes_per_element": 16, "what": "column-major <-> CAPS layout, n=%d, both directions" % n},
+        "sums": {"gbs": add_b / add_t / 1e9 if add_t > 0 else None,
+                 "frac_of_hbm_copy": (add_b / add_t / 1e9 / hbm_peak) if add_t > 0 else None,
+                 "what": "Strassen operand sums and C combinations of the timed multiplies (algorithmic bytes "
+                         "read + written / their kernels' CUDA-event time)"},
+        "hbm_copy_gbs": hbm_peak}
     s_used, nd_used, moduli = cnt["split_slices"], cnt["split_diagonals"], cnt["split_moduli"]
     value = replica_throughput(2.0 * n ** 3 / 1e12, world, t_split)
 
@@ -796,6 +824,7 @@ def main():
                          "avg_launch_ms": per_launch_s * 1e3,
                          "unit_of_work": unit_of_work},
             "cpu_baseline": cpu,
+            "memory_kernels": memory_kernels,
             "e2e": {"value": world * 2.0 * n ** 3 / t_e2e / 1e12, "unit": "TFLOP/s",
                     "h2d_bytes_per_step": 2 * n * n * 8, "d2h_bytes_per_step": n * n * 8,
                     "ms_per_step": t_e2e * 1e3, "step_ms": e2e_steps, "timeline": e2e_timeline,

@@ -290,9 +290,14 @@ cudaError_t launch_elementwise(int op, const EwTask *tasks, int count, int64_t q
 // 612-704) for one rank: nrec quadrant levels (TL, BL, TR, BR = offsets
 // 0,1,2,3 x quarter), then bs x bs column-major blocks, blocks column-major.
 //
-// One thread per element in CAPS order: consecutive CAPS indices are
-// consecutive rows of one column inside a block (runs of bs, or of the leaf
-// size when bs is 1 or the leaf), so both sides stay coalesced.
+// A block column is a run of bs consecutive doubles in the CAPS layout and
+// bs consecutive rows of one column of the column-major matrix: the reorder
+// is a copy of n^2 / bs runs.  A warp copies one run (runs of 32 and more:
+// the leaf columns when bs is 1 or the leaf, which is the workloads' case),
+// with 16-byte accesses when both ends of the run are 16-byte aligned; the
+// run's position is worked out once per run from its index (the quadrant
+// digits of its leaf, its block and column).  Shorter runs take one thread
+// per element.  HBM-bound either way: 16 bytes moved per element.
 // ---------------------------------------------------------------------------
 struct ReorderGeom {
     int64_t n, m, mm;   // matrix, leaf, leaf^2
@@ -301,9 +306,12 @@ struct ReorderGeom {
     int nb;             // blocks per leaf side
 };
 
-__device__ __forceinline__ int64_t caps_to_colmajor_index(const ReorderGeom &g, int64_t idx) {
-    int64_t leaf = idx / g.mm;
-    int64_t off = idx - leaf * g.mm;
+// column-major offset of the first element of run `run` (run = leaf * (mm /
+// bs) + blk * bs + cc: block blk of the leaf, column cc of the block)
+__device__ __forceinline__ int64_t run_colmajor_offset(const ReorderGeom &g, int64_t run) {
+    const int64_t runs_per_leaf = g.mm / g.bs;
+    const int64_t leaf = run / runs_per_leaf;
+    const int64_t rest = run - leaf * runs_per_leaf;
     int64_t r = 0, c = 0;
     for (int l = 0; l < g.nrec; l++) {
         int d = (int)((leaf >> (2 * (g.nrec - 1 - l))) & 3);
@@ -311,14 +319,49 @@ __device__ __forceinline__ int64_t caps_to_colmajor_index(const ReorderGeom &g, 
         r += (d & 1) * h;
         c += (d >> 1) * h;
     }
-    int64_t bs2 = (int64_t)g.bs * g.bs;
-    int64_t blk = off / bs2;
-    int64_t w = off - blk * bs2;
-    int64_t bj = blk % g.nb, bi = blk / g.nb;
-    int64_t cc = w / g.bs, rr = w - cc * g.bs;
-    r += bj * g.bs + rr;
+    const int64_t blk = rest / g.bs, cc = rest - blk * g.bs;
+    const int64_t bj = blk % g.nb, bi = blk / g.nb;  // block row, block column
+    r += bj * g.bs;
     c += bi * g.bs + cc;
     return r + c * g.n;
+}
+
+__device__ __forceinline__ int64_t caps_to_colmajor_index(const ReorderGeom &g, int64_t idx) {
+    const int64_t run = idx / g.bs;
+    return run_colmajor_offset(g, run) + (idx - run * g.bs);
+}
+
+// one warp per run of bs >= 32 doubles
+template <bool TO_CAPS>
+__device__ __forceinline__ void reorder_runs(const double *__restrict__ s, double *__restrict__ d,
+                                             const ReorderGeom &g, int64_t warp0, int64_t nwarps) {
+    const int lane = threadIdx.x & 31;
+    const int64_t runs = g.n * g.n / g.bs;
+    for (int64_t run = warp0; run < runs; run += nwarps) {
+        const int64_t cm = run_colmajor_offset(g, run), cp = run * g.bs;
+        const double *src = s + (TO_CAPS ? cm : cp);
+        double *dst = d + (TO_CAPS ? cp : cm);
+        if (((g.bs & 1) == 0) && (((uintptr_t)src | (uintptr_t)dst) & 15) == 0) {
+            const double2 *s2 = reinterpret_cast<const double2 *>(src);
+            double2 *d2 = reinterpret_cast<double2 *>(dst);
+            for (int64_t k = lane; k < g.bs / 2; k += 32) __stcs(d2 + k, __ldcs(s2 + k));
+        } else {
+            for (int64_t k = lane; k < g.bs; k += 32) __stcs(dst + k, __ldcs(src + k));
+        }
+    }
+}
+
+template <bool TO_CAPS>
+__device__ __forceinline__ void reorder_elements(const double *__restrict__ s, double *__restrict__ d,
+                                                 const ReorderGeom &g, int64_t t0, int64_t nthreads) {
+    const int64_t total = g.n * g.n;
+    for (int64_t idx = t0; idx < total; idx += nthreads) {
+        int64_t cm = caps_to_colmajor_index(g, idx);
+        if (TO_CAPS)
+            d[idx] = __ldcs(s + cm);
+        else
+            d[cm] = __ldcs(s + idx);
+    }
 }
 
 template <bool TO_CAPS>
@@ -327,15 +370,12 @@ __global__ void __launch_bounds__(256) reorder_kernel(const double *const *__res
                                                       ReorderGeom g) {
     const double *s = src[blockIdx.y];
     double *d = dst[blockIdx.y];
-    const int64_t total = g.n * g.n;
-    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        int64_t cm = caps_to_colmajor_index(g, idx);
-        if (TO_CAPS)
-            d[idx] = __ldcs(s + cm);
-        else
-            d[cm] = __ldcs(s + idx);
-    }
+    if (g.bs >= 32)
+        reorder_runs<TO_CAPS>(s, d, g, ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                              ((int64_t)gridDim.x * blockDim.x) >> 5);
+    else
+        reorder_elements<TO_CAPS>(s, d, g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                                  (int64_t)gridDim.x * blockDim.x);
 }
 
 static ReorderGeom make_geom(int64_t n, int nrec, int64_t bs) {
@@ -349,16 +389,23 @@ static ReorderGeom make_geom(int64_t n, int nrec, int64_t bs) {
     return g;
 }
 
+// grid: enough blocks for a run (or element) per thread, at most 8 blocks of
+// 256 threads per SM for all matrices together
+static unsigned reorder_blocks(const ReorderGeom &g, int count) {
+    const int64_t items = g.bs >= 32 ? g.n * g.n / g.bs * 32 : g.n * g.n;
+    int64_t blocks = (items + 255) / 256;
+    int64_t cap = (int64_t)152 * 8 / count;
+    if (cap < 1) cap = 1;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    return (unsigned)blocks;
+}
+
 cudaError_t launch_reorder(const double *const *src_dev, double *const *dst_dev, int count,
                            int64_t n, int nrec, int64_t bs, bool to_caps, cudaStream_t stream) {
     if (count <= 0) return cudaSuccess;
     ReorderGeom g = make_geom(n, nrec, bs);
-    int64_t total = n * n;
-    int64_t blocks = (total + 255) / 256;
-    int64_t cap = (int64_t)152 * 8 * 8 / count;
-    if (cap < 1) cap = 1;
-    if (blocks > cap) blocks = cap;
-    dim3 grid((unsigned)blocks, (unsigned)count);
+    dim3 grid(reorder_blocks(g, count), (unsigned)count);
     if (to_caps)
         reorder_kernel<true><<<grid, 256, 0, stream>>>(src_dev, dst_dev, g);
     else
@@ -370,28 +417,22 @@ cudaError_t launch_reorder(const double *const *src_dev, double *const *dst_dev,
 template <bool TO_CAPS>
 __global__ void __launch_bounds__(256) reorder_one_kernel(const double *__restrict__ s,
                                                           double *__restrict__ d, ReorderGeom g) {
-    const int64_t total = g.n * g.n;
-    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        int64_t cm = caps_to_colmajor_index(g, idx);
-        if (TO_CAPS)
-            d[idx] = __ldcs(s + cm);
-        else
-            d[cm] = __ldcs(s + idx);
-    }
+    if (g.bs >= 32)
+        reorder_runs<TO_CAPS>(s, d, g, ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                              ((int64_t)gridDim.x * blockDim.x) >> 5);
+    else
+        reorder_elements<TO_CAPS>(s, d, g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                                  (int64_t)gridDim.x * blockDim.x);
 }
 
 cudaError_t launch_reorder_one(const double *src, double *dst, int64_t n, int nrec, int64_t bs,
                                bool to_caps, cudaStream_t stream) {
     ReorderGeom g = make_geom(n, nrec, bs);
-    int64_t total = n * n;
-    int64_t blocks = (total + 255) / 256;
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    if (blocks < 1) blocks = 1;
+    const unsigned blocks = reorder_blocks(g, 1);
     if (to_caps)
-        reorder_one_kernel<true><<<(unsigned)blocks, 256, 0, stream>>>(src, dst, g);
+        reorder_one_kernel<true><<<blocks, 256, 0, stream>>>(src, dst, g);
     else
-        reorder_one_kernel<false><<<(unsigned)blocks, 256, 0, stream>>>(src, dst, g);
+        reorder_one_kernel<false><<<blocks, 256, 0, stream>>>(src, dst, g);
     count_launch();
     return cudaGetLastError();
 }
