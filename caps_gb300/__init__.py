@@ -43,7 +43,7 @@ C_ABI_SYMBOLS = [
     "caps_get_counters", "caps_reset_counters", "caps_set_phase_timing", "caps_multiply_batched_dev",
     "caps_status_string", "caps_last_cuda_error", "caps_debug_fail_allocations", "caps_release_cache",
     "caps_leaf_gemm_split_noalloc_dev", "caps_autotune_entry", "caps_chol_mult_dev", "caps_chol_mult_host",
-    "caps_debug_starve_split_gemm",
+    "caps_debug_starve_split_gemm", "caps_autotune_entry_ex",
 ]
 
 
@@ -142,6 +142,9 @@ def lib() -> ctypes.CDLL:
         ip = ctypes.POINTER(ctypes.c_int)
         L.caps_autotune_entry.argtypes = [ctypes.c_int, ip, ip, ip, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
         L.caps_autotune_entry.restype = ctypes.c_int
+        L.caps_autotune_entry_ex.argtypes = [ctypes.c_int, ip, ip, ip, ctypes.c_char_p, ip, ip,
+                                             ctypes.POINTER(ctypes.c_double)]
+        L.caps_autotune_entry_ex.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -285,16 +288,22 @@ def multiply_batched(As, Bs, Cs, ns, form: int | str = CAPS_FORM_PLAIN, slices: 
 
 
 def autotune_table() -> list:
-    """The autotuner's choices so far: dicts of n, form, nrec, pattern, seconds per instance."""
+    """The autotuner's choices so far: dicts of n, form, nrec, pattern, the
+    split scheme chosen ("residues" / "digits"; None for the plain form),
+    whether the entry came from the on-disk cache, and seconds per instance."""
     out = []
     i = 0
+    names = {0: None, 1: "digits", 2: "residues"}
     while True:
-        n, f, r, sec = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        n, f, r, sc, fc, sec = (ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int(),
+                                ctypes.c_double())
         pat = ctypes.create_string_buffer(9)
-        if lib().caps_autotune_entry(i, ctypes.byref(n), ctypes.byref(f), ctypes.byref(r), pat, ctypes.byref(sec)):
+        if lib().caps_autotune_entry_ex(i, ctypes.byref(n), ctypes.byref(f), ctypes.byref(r), pat, ctypes.byref(sc),
+                                        ctypes.byref(fc), ctypes.byref(sec)):
             return out
         out.append({"n": n.value, "form": "split" if f.value == 1 else "plain", "nrec": r.value,
-                    "pattern": pat.value.decode(), "seconds_per_instance": sec.value})
+                    "pattern": pat.value.decode(), "scheme": names.get(sc.value, sc.value),
+                    "from_cache": bool(fc.value), "seconds_per_instance": sec.value})
         i += 1
 
 

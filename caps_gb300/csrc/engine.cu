@@ -28,6 +28,8 @@
 #include <string>
 #include <vector>
 
+#include <sys/stat.h>
+
 namespace caps {
 
 // ------------------------------------------------------------------ state
@@ -828,7 +830,9 @@ struct TuneEntry {
     int nrec;
     char pat[8];
     double seconds;
-    int scheme;
+    int scheme;         // the split scheme asked for (caps_options.split_scheme)
+    int chosen_scheme;  // the split scheme that won (the plain form: 0)
+    int from_cache;     // 1: read from the on-disk cache, not timed in this process
 };
 static std::vector<TuneEntry> g_tune;
 
@@ -878,6 +882,7 @@ static int64_t batch_ws_per_instance(int n, int nrec, const char *pat, int form,
 struct ClassCfg {
     int n, nrec;
     char pat[8];
+    int scheme;  // split form: the scheme the class runs with (caps_split_scheme)
 };
 
 // Appends the ops of a batch to the builder.
@@ -916,7 +921,10 @@ static void build_batch(Builder &b, const std::vector<BatchItem> &items, const s
                 emit_reorder(b, ra, da, c.n, 1, true, c.nrec);
                 emit_reorder(b, rb, db, c.n, 1, true, c.nrec);
             }
+            const int asked = b.opt.split_scheme;
+            if (b.opt.form == CAPS_FORM_SPLIT) b.opt.split_scheme = c.scheme;
             build(b, P, c.n, c.nrec, c.pat);
+            b.opt.split_scheme = asked;
             if (c.nrec > 0) emit_reorder(b, rc_src, rc_dst, c.n, 1, false, c.nrec);
             b.release(mk);
         }
@@ -964,16 +972,108 @@ static caps_status run_plan_direct(BatchPlan &p, cudaStream_t s) {
     return launch_ops(p.ops, tables, p.buf.ptr, s, nullptr, nullptr);
 }
 
-// Autotuner: for one size and form, times each candidate depth / pattern on
-// a synthetic batch of that size and keeps the fastest (cached per process).
+// Autotuner: for one size and form, times each candidate on a synthetic batch
+// of that size and keeps the fastest.  Candidates: recursion depth 0..3 (as
+// the leaves allow), the b/d pattern of the top step, and for the split
+// form with an automatic scheme the operand cut (residues when the leaves
+// fit them, digits).  Tile shapes are fixed per kernel (residue GEMM 128 x
+// 256, digit GEMM 128 x 64, DMMA 64 x 64), so they are not an axis.  The
+// choices are kept per process and in an on-disk cache (see tune_cache_*).
+
+// On-disk cache of the tuner's choices: one tab-separated line per choice,
+// keyed by the tuning version, the device's name and SM count, the size,
+// form, slices and asked-for scheme.  The file is CAPS_AUTOTUNE_CACHE if set
+// (empty: no disk cache), else $HOME/.cache/caps_gb300/autotune.tsv.  A new
+// tuning version (a change of the kernels the choices were timed with)
+// leaves older lines unused; deleting the file forces new timings.
+static const char *kTuneVersion = "caps-tune-2";
+
+static std::string tune_cache_path() {
+    const char *e = getenv("CAPS_AUTOTUNE_CACHE");
+    if (e) return std::string(e);
+    const char *home = getenv("HOME");
+    if (!home || !*home) return std::string();
+    return std::string(home) + "/.cache/caps_gb300/autotune.tsv";
+}
+
+static std::string tune_device_key() {
+    int dev = 0;
+    cudaDeviceProp prop;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return std::string();
+    }
+    std::string name(prop.name);
+    for (char &c : name)
+        if (c == '\t' || c == ' ') c = '_';
+    return name + "/" + std::to_string(prop.multiProcessorCount);
+}
+
+static bool tune_cache_lookup(int n, const caps_options &o, TuneEntry &out) {
+    const std::string path = tune_cache_path(), dev = tune_device_key();
+    if (path.empty() || dev.empty()) return false;
+    FILE *f = fopen(path.c_str(), "r");
+    if (!f) return false;
+    char ver[64], dk[256], pat[16];
+    int fn, fform, fslices, fscheme, nrec, chosen;
+    double sec;
+    bool found = false;
+    while (fscanf(f, "%63s %255s %d %d %d %d %d %15s %d %lf", ver, dk, &fn, &fform, &fslices, &fscheme, &nrec, pat,
+                  &chosen, &sec) == 10) {
+        if (strcmp(ver, kTuneVersion) || dev != dk || fn != n || fform != o.form || fslices != o.slices ||
+            fscheme != o.split_scheme || nrec < 0 || nrec > 3)
+            continue;
+        TuneEntry t{n, o.form, o.slices, nrec, {0}, sec, o.split_scheme, chosen, 1};
+        if (strcmp(pat, "-")) memcpy(t.pat, pat, std::min<size_t>(strlen(pat), 7));
+        out = t;
+        found = true;  // the last matching line wins
+    }
+    fclose(f);
+    return found;
+}
+
+static void tune_cache_store(const TuneEntry &t) {
+    const std::string path = tune_cache_path(), dev = tune_device_key();
+    if (path.empty() || dev.empty()) return;
+    const size_t slash = path.rfind('/');
+    if (slash != std::string::npos && slash > 0) {
+        // the cache's directory and its parent (e.g. ~/.cache/caps_gb300)
+        const std::string dir = path.substr(0, slash);
+        struct stat sb;
+        if (stat(dir.c_str(), &sb) != 0) {
+            const size_t up = dir.rfind('/');
+            if (up != std::string::npos && up > 0 && stat(dir.substr(0, up).c_str(), &sb) != 0)
+                mkdir(dir.substr(0, up).c_str(), 0755);
+            mkdir(dir.c_str(), 0755);
+        }
+    }
+    FILE *f = fopen(path.c_str(), "a");
+    if (!f) return;
+    fprintf(f, "%s\t%s\t%d\t%d\t%d\t%d\t%d\t%s\t%d\t%.9g\n", kTuneVersion, dev.c_str(), t.n, t.form, t.slices,
+            t.scheme, t.nrec, t.pat[0] ? t.pat : "-", t.chosen_scheme, t.seconds);
+    fclose(f);
+}
+
 static caps_status tune_size(int n, const caps_options &o, ClassCfg &out) {
     for (const TuneEntry &t : g_tune)
         if (t.n == n && t.form == o.form && t.slices == o.slices && t.scheme == o.split_scheme) {
             out.n = n;
             out.nrec = t.nrec;
             memcpy(out.pat, t.pat, sizeof out.pat);
+            out.scheme = t.chosen_scheme;
             return CAPS_OK;
         }
+    {
+        TuneEntry cached;
+        if (tune_cache_lookup(n, o, cached)) {
+            g_tune.push_back(cached);
+            out.n = n;
+            out.nrec = cached.nrec;
+            memcpy(out.pat, cached.pat, sizeof out.pat);
+            out.scheme = cached.chosen_scheme;
+            return CAPS_OK;
+        }
+    }
     int rmax = max_tune_nrec(n, o.form);
     int T = (int)std::max<int64_t>(1, std::min<int64_t>(32, ((int64_t)1 << 27) / ((int64_t)n * n)));
     int64_t nn = (int64_t)n * n;
@@ -982,34 +1082,42 @@ static caps_status tune_size(int n, const caps_options &o, ClassCfg &out) {
     fill_uniform_kernel<<<1024, 256>>>(data, 3 * nn * T, 12345 + n);
     std::vector<BatchItem> items;
     for (int i = 0; i < T; i++) items.push_back({n, data + 3 * nn * i, data + 3 * nn * i + nn, data + 3 * nn * i + 2 * nn});
-    ClassCfg best{n, 0, {0}};
+    ClassCfg best{n, 0, {0}, o.split_scheme};
     double best_t = 1e30;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     caps_status st = CAPS_OK;
+    // split form, scheme left to the library: time both cuts (residues only
+    // where the leaves fit them; otherwise they would run as digits anyway)
+    const bool both = o.form == CAPS_FORM_SPLIT && o.split_scheme == CAPS_SPLIT_AUTO && o.slices == 0;
     for (int r = 0; r <= rmax && st == CAPS_OK; r++) {
-        for (int variant = 0; variant < (r >= 2 ? 2 : 1); variant++) {
-            ClassCfg c{n, r, {0}};
-            for (int k = 0; k < r; k++) c.pat[k] = (variant == 1 && k == 0) ? 'd' : 'b';
-            BatchPlan p;
-            p.items = items;
-            st = plan_batch(p, {c}, o);
-            if (st != CAPS_OK) { if (p.buf.ptr) cudaFree(p.buf.ptr); break; }
-            double t = 1e30;
-            for (int rep = 0; rep < 3 && st == CAPS_OK; rep++) {
-                cudaEventRecord(e0, 0);
-                st = run_plan_direct(p, 0);
-                cudaEventRecord(e1, 0);
-                if (cudaEventSynchronize(e1) != cudaSuccess) st = CAPS_ERR_CUDA;
-                float ms = 0;
-                cudaEventElapsedTime(&ms, e0, e1);
-                if (rep > 0) t = std::min(t, (double)ms);
-            }
-            if (p.buf.ptr) cudaFree(p.buf.ptr);
-            if (st == CAPS_OK && t < best_t) {
-                best_t = t;
-                best = c;
+        const int leaf = n >> r;
+        for (int sc = 0; sc < (both ? 2 : 1) && st == CAPS_OK; sc++) {
+            const int scheme = both ? (sc == 0 ? CAPS_SPLIT_RESIDUES : CAPS_SPLIT_DIGITS) : o.split_scheme;
+            if (both && scheme == CAPS_SPLIT_RESIDUES && (leaf + 15) / 16 * 16 > 2048) continue;
+            for (int variant = 0; variant < (r >= 2 ? 2 : 1); variant++) {
+                ClassCfg c{n, r, {0}, scheme};
+                for (int k = 0; k < r; k++) c.pat[k] = (variant == 1 && k == 0) ? 'd' : 'b';
+                BatchPlan p;
+                p.items = items;
+                st = plan_batch(p, {c}, o);
+                if (st != CAPS_OK) { if (p.buf.ptr) cudaFree(p.buf.ptr); break; }
+                double t = 1e30;
+                for (int rep = 0; rep < 3 && st == CAPS_OK; rep++) {
+                    cudaEventRecord(e0, 0);
+                    st = run_plan_direct(p, 0);
+                    cudaEventRecord(e1, 0);
+                    if (cudaEventSynchronize(e1) != cudaSuccess) st = CAPS_ERR_CUDA;
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (rep > 0) t = std::min(t, (double)ms);
+                }
+                if (p.buf.ptr) cudaFree(p.buf.ptr);
+                if (st == CAPS_OK && t < best_t) {
+                    best_t = t;
+                    best = c;
+                }
             }
         }
     }
@@ -1017,9 +1125,11 @@ static caps_status tune_size(int n, const caps_options &o, ClassCfg &out) {
     cudaEventDestroy(e1);
     cudaFree(data);
     if (st != CAPS_OK) return st;
-    TuneEntry te{n, o.form, o.slices, best.nrec, {0}, best_t / 1e3 / T, o.split_scheme};
+    TuneEntry te{n, o.form, o.slices, best.nrec, {0}, best_t / 1e3 / T, o.split_scheme,
+                 o.form == CAPS_FORM_SPLIT ? best.scheme : 0, 0};
     memcpy(te.pat, best.pat, sizeof te.pat);
     g_tune.push_back(te);
+    tune_cache_store(te);
     out = best;
     return CAPS_OK;
 }
@@ -1394,6 +1504,11 @@ caps_status caps_multiply_batched_dev(int count, const double *const *A, const d
 }
 
 caps_status caps_autotune_entry(int index, int *n, int *form, int *nrec, char *pattern, double *seconds) {
+    return caps_autotune_entry_ex(index, n, form, nrec, pattern, nullptr, nullptr, seconds);
+}
+
+caps_status caps_autotune_entry_ex(int index, int *n, int *form, int *nrec, char *pattern, int *scheme,
+                                   int *from_cache, double *seconds) {
     std::lock_guard<std::recursive_mutex> g(g_mu);
     if (index < 0 || index >= (int)g_tune.size()) return CAPS_ERR_ARG;
     const TuneEntry &t = g_tune[index];
@@ -1401,6 +1516,8 @@ caps_status caps_autotune_entry(int index, int *n, int *form, int *nrec, char *p
     if (form) *form = t.form;
     if (nrec) *nrec = t.nrec;
     if (pattern) memcpy(pattern, t.pat, sizeof t.pat);
+    if (scheme) *scheme = t.chosen_scheme;
+    if (from_cache) *from_cache = t.from_cache;
     if (seconds) *seconds = t.seconds;
     return CAPS_OK;
 }

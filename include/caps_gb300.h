@@ -203,8 +203,21 @@ caps_status caps_multiply_batched_dev(int count, const double *const *A, const d
 
 /* Autotuner choices made so far: entry `index` (0, 1, ...) gives the size,
  * form, recursion depth, pattern (8 bytes) and seconds per instance of the
- * winning candidate; CAPS_ERR_ARG past the last entry. */
+ * winning candidate; CAPS_ERR_ARG past the last entry.  No reference
+ * counterpart. */
 caps_status caps_autotune_entry(int index, int *n, int *form, int *nrec, char *pattern, double *seconds);
+
+/* The same with the split scheme the tuner chose (caps_split_scheme; 0 for
+ * the plain form) and whether the entry was read from the on-disk cache (1)
+ * or timed in this process (0).  The tuner searches recursion depth (0..3,
+ * as the leaves allow), the top step's b/d pattern and, for the split form
+ * with an automatic scheme, residues against digits.  Its choices are kept
+ * in CAPS_AUTOTUNE_CACHE (a file; empty: no cache) or by default in
+ * $HOME/.cache/caps_gb300/autotune.tsv, keyed by the device's name and SM
+ * count, the size, form, slices and asked-for scheme.  Tile shapes are fixed
+ * per kernel.  Any pointer may be NULL. */
+caps_status caps_autotune_entry_ex(int index, int *n, int *form, int *nrec, char *pattern, int *scheme,
+                                   int *from_cache, double *seconds);
 
 /* Human-readable text of a status. */
 const char *caps_status_string(caps_status s);

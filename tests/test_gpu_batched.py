@@ -62,3 +62,41 @@ def test_batched_argument_errors(caps, cuda):
     with pytest.raises(caps.CapsError) as e:
         caps.multiply_batched([t], [t], [t], [0])
     assert e.value.status == 2
+
+
+def test_autotune_choices_persist_on_disk(caps, cuda, tmp_path):
+    """Two fresh processes with the same CAPS_AUTOTUNE_CACHE file: the first
+    times the candidates and writes its choices, the second reads them back
+    (from_cache) and makes the same ones; both give exact integer products."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cache = tmp_path / "autotune.tsv"
+    code = (
+        "import sys, json, numpy as np, torch; sys.path.insert(0, %r); import caps_gb300 as cg; "
+        "sizes = [448, 224]; rng = np.random.default_rng(3); ok = True; As = []; Bs = []; Cs = []; ref = []\n"
+        "for n in sizes:\n"
+        "    A = rng.integers(-9, 10, (n, n)).astype(np.float64); B = rng.integers(-9, 10, (n, n)).astype(np.float64)\n"
+        "    As.append(torch.from_numpy(A.T.copy().reshape(-1)).cuda()); Bs.append(torch.from_numpy(B.T.copy().reshape(-1)).cuda())\n"
+        "    Cs.append(torch.empty(n * n, dtype=torch.float64, device='cuda')); ref.append(A.astype(np.int64) @ B.astype(np.int64))\n"
+        "cg.multiply_batched(As, Bs, Cs, sizes, form='split'); torch.cuda.synchronize()\n"
+        "for C, R, n in zip(Cs, ref, sizes): ok = ok and np.array_equal(C.cpu().numpy().reshape(n, n).T, R.astype(np.float64))\n"
+        "print(json.dumps({'ok': bool(ok), 'tab': cg.autotune_table()}))\n" % root)
+    env = dict(os.environ, CAPS_AUTOTUNE_CACHE=str(cache))
+    runs = []
+    for _ in range(2):
+        out = subprocess.run([sys.executable, "-c", code], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                             text=True, timeout=600, env=env)
+        assert out.returncode == 0, out.stdout
+        runs.append(json.loads(out.stdout.strip().splitlines()[-1]))
+    assert runs[0]["ok"] and runs[1]["ok"]
+    assert cache.exists() and len(cache.read_text().strip().splitlines()) >= 2
+    first = {t["n"]: t for t in runs[0]["tab"]}
+    second = {t["n"]: t for t in runs[1]["tab"]}
+    assert set(first) == set(second) == {448, 224}
+    for n in first:
+        assert not first[n]["from_cache"] and second[n]["from_cache"]
+        for k in ("nrec", "pattern", "scheme"):
+            assert first[n][k] == second[n][k], (n, k)
