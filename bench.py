@@ -379,7 +379,7 @@ def run_batched512(args, world, rank, local):
                                      res["split"]["value"], args, world, res["split"]["ms_per_step"],
                                      {"workload": "512 independent multiplies, n over {448,896,1792,3584}",
                                       "sizes": counts, "form": "split", "inputs": "uniform[-1,1) seeded",
-                                      "execution": "per-size autotuned depth/pattern, CUDA graph replay"},
+                                      "execution": "per-size autotuned depth/pattern/scheme, CUDA graph replay"},
                                      split=res["split"], plain_fp64=res["plain"],
                                      split_vs_plain=res["split"]["value"] / res["plain"]["value"],
                                      autotune=cg.autotune_table(), clocks=res["split"]["clocks"],
