@@ -43,7 +43,7 @@ C_ABI_SYMBOLS = [
     "caps_get_counters", "caps_reset_counters", "caps_set_phase_timing", "caps_multiply_batched_dev",
     "caps_status_string", "caps_last_cuda_error", "caps_debug_fail_allocations", "caps_release_cache",
     "caps_leaf_gemm_split_noalloc_dev", "caps_autotune_entry", "caps_chol_mult_dev", "caps_chol_mult_host",
-    "caps_debug_starve_split_gemm", "caps_autotune_entry_ex",
+    "caps_debug_starve_split_gemm", "caps_autotune_entry_ex", "caps_autotune_info",
 ]
 
 
@@ -66,10 +66,19 @@ class MatDescriptor(ctypes.Structure):
         return cls(lda, nrec, 1, 1, 1, int(hybrid), bs)
 
 
+class TuneInfo(ctypes.Structure):
+    """caps_tune_info: one autotuner choice with all its axes."""
+    _fields_ = [("n", ctypes.c_int), ("form", ctypes.c_int), ("nrec", ctypes.c_int), ("pattern", ctypes.c_char * 8),
+                ("scheme", ctypes.c_int), ("tile_rows", ctypes.c_int), ("tile_cols", ctypes.c_int),
+                ("operand_bits", ctypes.c_int), ("moduli", ctypes.c_int), ("gate_rejected", ctypes.c_int),
+                ("from_cache", ctypes.c_int), ("seconds", ctypes.c_double)]
+
+
 class Options(ctypes.Structure):
     _fields_ = [("form", ctypes.c_int), ("slices", ctypes.c_int), ("diagonals", ctypes.c_int),
                 ("split_scheme", ctypes.c_int), ("workspace_limit", ctypes.c_longlong),
-                ("reserved", ctypes.c_longlong * 4)]
+                ("plain_tile", ctypes.c_int), ("operand_bits", ctypes.c_int),
+                ("reserved", ctypes.c_longlong * 3)]
 
 
 class Counters(ctypes.Structure):
@@ -145,6 +154,8 @@ def lib() -> ctypes.CDLL:
         L.caps_autotune_entry_ex.argtypes = [ctypes.c_int, ip, ip, ip, ctypes.c_char_p, ip, ip,
                                              ctypes.POINTER(ctypes.c_double)]
         L.caps_autotune_entry_ex.restype = ctypes.c_int
+        L.caps_autotune_info.argtypes = [ctypes.c_int, ctypes.POINTER(TuneInfo)]
+        L.caps_autotune_info.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -162,8 +173,14 @@ def _check(status: int) -> None:
 SPLIT_SCHEMES = {"auto": 0, "digits": 1, "residues": 2}
 
 
+PLAIN_TILES = {"64x64": 0, "32x32": 1, "128x64": 2}
+
+
 def options(form: int | str = CAPS_FORM_PLAIN, slices: int = 0, diagonals: int = 0,
-            workspace_limit: int = 0, scheme: int | str = 0) -> Options:
+            workspace_limit: int = 0, scheme: int | str = 0, tile: int | str = 0,
+            operand_bits: int = 0) -> Options:
+    """caps_options.  tile: the plain form's DMMA tile ("64x64", "32x32",
+    "128x64"); operand_bits: the residue scheme's operand-bit cap (0 = 55)."""
     if isinstance(form, str):
         form = {"plain": CAPS_FORM_PLAIN, "split": CAPS_FORM_SPLIT}[form]
     if isinstance(scheme, str):
@@ -172,6 +189,8 @@ def options(form: int | str = CAPS_FORM_PLAIN, slices: int = 0, diagonals: int =
     lib().caps_options_init(ctypes.byref(o))
     o.form, o.slices, o.diagonals, o.workspace_limit = int(form), int(slices), int(diagonals), int(workspace_limit)
     o.split_scheme = int(scheme)
+    o.plain_tile = PLAIN_TILES[tile] if isinstance(tile, str) else int(tile)
+    o.operand_bits = int(operand_bits)
     return o
 
 
@@ -199,15 +218,15 @@ def _stream_ptr(stream):
 
 def multiply(A, B, C, desc: MatDescriptor, pattern=None, form: int | str = CAPS_FORM_PLAIN,
              slices: int = 0, diagonals: int = 0, workspace_limit: int = 0, stream=None,
-             scheme: int | str = 0) -> None:
+             scheme: int | str = 0, tile: int | str = 0, operand_bits: int = 0) -> None:
     """C = A * B for CAPS-layout matrices (multiply.h:13).
 
     Torch CUDA tensors run asynchronously on `stream` (default: torch's
     current stream); numpy arrays go through the host entry point, which
     stages the copies and synchronises.  scheme: split-form operand cut
-    ("auto", "digits" or "residues").
+    ("auto", "digits" or "residues"); tile, operand_bits: see options().
     """
-    opt = options(form, slices, diagonals, workspace_limit, scheme)
+    opt = options(form, slices, diagonals, workspace_limit, scheme, tile, operand_bits)
     if isinstance(A, np.ndarray):
         for x in (A, B, C):
             if x.dtype != np.float64 or not x.flags.c_contiguous:
@@ -221,9 +240,9 @@ def multiply(A, B, C, desc: MatDescriptor, pattern=None, form: int | str = CAPS_
 
 
 def leaf_gemm(A, B, C, m: int, form: int | str = CAPS_FORM_PLAIN, slices: int = 0, diagonals: int = 0,
-              stream=None, scheme: int | str = 0) -> None:
+              stream=None, scheme: int | str = 0, tile: int | str = 0, operand_bits: int = 0) -> None:
     """Base case alone: column-major m x m C = A * B on the device."""
-    opt = options(form, slices, diagonals, 0, scheme)
+    opt = options(form, slices, diagonals, 0, scheme, tile, operand_bits)
     _check(lib().caps_leaf_gemm_dev(_dev_ptr(A, "A"), _dev_ptr(B, "B"), _dev_ptr(C, "C"), int(m),
                                     ctypes.byref(opt), _stream_ptr(stream)))
 
@@ -288,22 +307,23 @@ def multiply_batched(As, Bs, Cs, ns, form: int | str = CAPS_FORM_PLAIN, slices: 
 
 
 def autotune_table() -> list:
-    """The autotuner's choices so far: dicts of n, form, nrec, pattern, the
-    split scheme chosen ("residues" / "digits"; None for the plain form),
-    whether the entry came from the on-disk cache, and seconds per instance."""
+    """The autotuner's choices so far (caps_autotune_info): dicts of n, form,
+    nrec, pattern, the split scheme chosen ("residues" / "digits"; None for
+    the plain form), the base-case tile, the residues' operand bits and
+    moduli (0 otherwise), the bit caps the accuracy gate turned down, whether
+    the entry came from the on-disk cache, and seconds per instance."""
     out = []
     i = 0
     names = {0: None, 1: "digits", 2: "residues"}
     while True:
-        n, f, r, sc, fc, sec = (ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int(),
-                                ctypes.c_double())
-        pat = ctypes.create_string_buffer(9)
-        if lib().caps_autotune_entry_ex(i, ctypes.byref(n), ctypes.byref(f), ctypes.byref(r), pat, ctypes.byref(sc),
-                                        ctypes.byref(fc), ctypes.byref(sec)):
+        t = TuneInfo()
+        if lib().caps_autotune_info(i, ctypes.byref(t)):
             return out
-        out.append({"n": n.value, "form": "split" if f.value == 1 else "plain", "nrec": r.value,
-                    "pattern": pat.value.decode(), "scheme": names.get(sc.value, sc.value),
-                    "from_cache": bool(fc.value), "seconds_per_instance": sec.value})
+        out.append({"n": t.n, "form": "split" if t.form == 1 else "plain", "nrec": t.nrec,
+                    "pattern": t.pattern.decode(), "scheme": names.get(t.scheme, t.scheme),
+                    "tile": [t.tile_rows, t.tile_cols], "operand_bits": t.operand_bits, "moduli": t.moduli,
+                    "gate_rejected": t.gate_rejected, "from_cache": bool(t.from_cache),
+                    "seconds_per_instance": t.seconds})
         i += 1
 
 

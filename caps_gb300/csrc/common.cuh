@@ -105,8 +105,12 @@ struct LeafTask {
     double *C;
 };
 
-// FP64 DMMA GEMM (mma.sync f64): C = A * B for every task.
-cudaError_t launch_dmma_gemm(const LeafTask *tasks_dev, int count, int m, cudaStream_t stream);
+// FP64 DMMA GEMM (mma.sync f64): C = A * B for every task, in CTA tiles of
+// one of three shapes (an autotuner axis).
+enum DmmaTile { DMMA_TILE_64x64 = 0, DMMA_TILE_32x32 = 1, DMMA_TILE_128x64 = 2, DMMA_TILES = 3 };
+void dmma_tile_shape(int tile, int *rows, int *cols);
+cudaError_t launch_dmma_gemm(const LeafTask *tasks_dev, int count, int m, cudaStream_t stream,
+                             int tile = DMMA_TILE_64x64);
 
 // Split form.  Two schemes share one launch sequence; the kernels agree on
 // the scheme through the launch group's header, written on the device after
@@ -120,8 +124,14 @@ struct SplitParams {
     int slices;     // digit scheme: digits per operand, 1..8 (0 = from the data)
     int diagonals;  // digit scheme: digit-pair diagonals kept, <= 8, >= slices
     int scheme;     // caps_options.split_scheme: 0 automatic, 1 digits, 2 residues
+    int bits;       // residue scheme: cap on the operand bits t_a, t_b (0 = 55); fewer
+                    // bits need fewer moduli (an autotuner axis, gated on accuracy)
 };
 size_t split_workspace_bytes(int m, int count, int scheme);
+constexpr int RESIDUE_KMAX = 2048;  // residue scheme: largest leaf K (K 90^2 < 2^24, exact fp32 sums)
+// Moduli the residue scheme takes for operands of `bits` bits at inner
+// dimension K (0 if more than it has).
+int crt_moduli_needed(int bits, int K);
 // Computes per-row / per-column scale exponents and the needed digit count.
 cudaError_t launch_split_scan(const LeafTask *tasks_dev, int count, int m, SplitParams p, void *workspace,
                              cudaStream_t stream);

@@ -140,6 +140,7 @@ struct Op {
     bool to_caps;
     size_t split_off;  // workspace offset of the split scratch
     SplitParams sp;
+    int tile;          // K_LEAF_DMMA: CTA tile shape (DmmaTile)
 };
 
 struct Prob {
@@ -251,6 +252,7 @@ static void emit_leaf_gemm(Builder &b, const std::vector<Prob> &P, int64_t m) {
             o.sp.slices = b.opt.slices;
             o.sp.diagonals = b.opt.diagonals;
             o.sp.scheme = scheme;
+            o.sp.bits = b.opt.operand_bits;
             b.ops.push_back(o);
         }
     } else {
@@ -260,6 +262,7 @@ static void emit_leaf_gemm(Builder &b, const std::vector<Prob> &P, int64_t m) {
         o.kind = K_LEAF_DMMA;
         o.count = (int)t.size();
         o.m = (int)m;
+        o.tile = b.opt.plain_tile;
         o.toff = b.table(t);
         b.ops.push_back(o);
     }
@@ -505,6 +508,8 @@ static caps_status check_opts(const caps_options &o) {
     if (o.slices < 0 || o.slices > 8) return CAPS_ERR_ARG;
     if (o.diagonals < 0 || o.diagonals > 8) return CAPS_ERR_ARG;
     if (o.split_scheme < CAPS_SPLIT_AUTO || o.split_scheme > CAPS_SPLIT_RESIDUES) return CAPS_ERR_ARG;
+    if (o.plain_tile < CAPS_TILE_64x64 || o.plain_tile > CAPS_TILE_128x64) return CAPS_ERR_ARG;
+    if (o.operand_bits < 0 || o.operand_bits > 55) return CAPS_ERR_ARG;
     return CAPS_OK;
 }
 
@@ -648,7 +653,7 @@ static caps_status launch_ops(const std::vector<Op> &ops, char *tables, char *ws
                 break;
             case K_LEAF_DMMA:
                 if (timed) ev_begin(r.e0);
-                err = launch_dmma_gemm(reinterpret_cast<const LeafTask *>(tables + o.toff), o.count, o.m, s);
+                err = launch_dmma_gemm(reinterpret_cast<const LeafTask *>(tables + o.toff), o.count, o.m, s, o.tile);
                 r.phase = PH_MUL;
                 r.gemm = true;
                 r.m3 = (double)o.count * o.m * (double)o.m * o.m;
@@ -833,6 +838,9 @@ struct TuneEntry {
     int scheme;         // the split scheme asked for (caps_options.split_scheme)
     int chosen_scheme;  // the split scheme that won (the plain form: 0)
     int from_cache;     // 1: read from the on-disk cache, not timed in this process
+    int tile;           // plain form: the DMMA tile that won (DmmaTile)
+    int bits;           // split form, residues: the operand-bit cap that won (0 = 55)
+    int rejected;       // smaller caps that were faster but failed the accuracy gate
 };
 static std::vector<TuneEntry> g_tune;
 
@@ -883,6 +891,8 @@ struct ClassCfg {
     int n, nrec;
     char pat[8];
     int scheme;  // split form: the scheme the class runs with (caps_split_scheme)
+    int tile;    // plain form: base-case CTA tile (DmmaTile)
+    int bits;    // split form, residues: operand-bit cap (0 = 55)
 };
 
 // Appends the ops of a batch to the builder.
@@ -923,8 +933,13 @@ static void build_batch(Builder &b, const std::vector<BatchItem> &items, const s
             }
             const int asked = b.opt.split_scheme;
             if (b.opt.form == CAPS_FORM_SPLIT) b.opt.split_scheme = c.scheme;
+            const int tile = b.opt.plain_tile, bits = b.opt.operand_bits;
+            b.opt.plain_tile = c.tile;
+            b.opt.operand_bits = c.bits;
             build(b, P, c.n, c.nrec, c.pat);
             b.opt.split_scheme = asked;
+            b.opt.plain_tile = tile;
+            b.opt.operand_bits = bits;
             if (c.nrec > 0) emit_reorder(b, rc_src, rc_dst, c.n, 1, false, c.nrec);
             b.release(mk);
         }
@@ -956,13 +971,49 @@ static caps_status plan_batch(BatchPlan &p, const std::vector<ClassCfg> &cfg, co
     return CAPS_OK;
 }
 
-__global__ void fill_uniform_kernel(double *p, int64_t n, uint64_t seed) {
+// Tuning data: uniform [-1, 1), or with `wide` set the same times 2^k, k
+// uniform in [-20, 20] (entries spanning 40 binades, the hard case for a
+// truncated operand cut).
+__global__ void fill_uniform_kernel(double *p, int64_t n, uint64_t seed, int wide) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         uint64_t z = (uint64_t)i * 0x9E3779B97F4A7C15ull + seed;
         z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
         z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
         z ^= z >> 31;
-        p[i] = (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+        double v = (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+        if (wide) v = ldexp(v, (int)((z & 0xFFFFu) % 41u) - 20);
+        p[i] = v;
+    }
+}
+
+// Error sums of the tuner's accuracy gate over T instances (C of instance i
+// at c + i * cstride, its reference at r + i * nn): out[0] += sum (c - r)^2,
+// out[1] += sum r^2, out[2] = max |c - r| (infinite where c is not a
+// number), out[3] = max |r|.  out[2], out[3] are non-negative doubles, whose
+// encodings order as the values do.
+__global__ void tune_error_kernel(const double *__restrict__ c, const double *__restrict__ r, int64_t nn, int T,
+                                  int64_t cstride, double *out) {
+    double s2 = 0, r2 = 0, md = 0, mr = 0;
+    const int64_t total = nn * T;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = k / nn, e = k - i * nn;
+        const double y = r[k], d = c[i * cstride + e] - y, ad = fabs(d);
+        s2 += d * d;
+        r2 += y * y;
+        md = ad == ad ? fmax(md, ad) : INFINITY;
+        mr = fmax(mr, fabs(y));
+    }
+    for (int o = 16; o; o >>= 1) {
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+        md = fmax(md, __shfl_xor_sync(0xffffffffu, md, o));
+        mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out, s2);
+        atomicAdd(out + 1, r2);
+        atomicMax(reinterpret_cast<unsigned long long *>(out + 2), (unsigned long long)__double_as_longlong(md));
+        atomicMax(reinterpret_cast<unsigned long long *>(out + 3), (unsigned long long)__double_as_longlong(mr));
     }
 }
 
@@ -972,21 +1023,31 @@ static caps_status run_plan_direct(BatchPlan &p, cudaStream_t s) {
     return launch_ops(p.ops, tables, p.buf.ptr, s, nullptr, nullptr);
 }
 
-// Autotuner: for one size and form, times each candidate on a synthetic batch
-// of that size and keeps the fastest.  Candidates: recursion depth 0..3 (as
-// the leaves allow), the b/d pattern of the top step, and for the split
-// form with an automatic scheme the operand cut (residues when the leaves
-// fit them, digits).  Tile shapes are fixed per kernel (residue GEMM 128 x
-// 256, digit GEMM 128 x 64, DMMA 64 x 64), so they are not an axis.  The
-// choices are kept per process and in an on-disk cache (see tune_cache_*).
+// Autotuner: for one size and form, times candidates on a synthetic batch of
+// that size and keeps the fastest.  Axes, searched in turn (each at the best
+// point of the ones before it):
+//   1. recursion depth 0..3 (as the leaves allow) and the b/d pattern of the
+//      top step; for the split form with the scheme left to the library, also
+//      the operand cut (residues where the leaves fit them, digits);
+//   2. plain form: the DMMA CTA tile (64 x 64, 32 x 32, 128 x 64);
+//   3. split form, where the residues won: the operand-bit cap, 55 / 52 / 48
+//      bits (17 / 16 / 15 moduli at K <= 2048: fewer modular products and
+//      residue planes).  A smaller cap is kept only if it is faster and, on
+//      the uniform batch and on a wide-range batch (u 2^k, k in [-20, 20]),
+//      its error against a split reference (depth 0, 55 bits) is no larger
+//      than the plain FP64 form's at the same depth and pattern, both
+//      normwise and in the largest entry.
+// The split GEMMs' tiles (residues 128 x 256, digits 128 x 64) are fixed:
+// the operand slicers write their planes in those tiles' layout.  The
+// choices are kept per process and in an on-disk cache (tune_cache_*).
 
 // On-disk cache of the tuner's choices: one tab-separated line per choice,
 // keyed by the tuning version, the device's name and SM count, the size,
 // form, slices and asked-for scheme.  The file is CAPS_AUTOTUNE_CACHE if set
 // (empty: no disk cache), else $HOME/.cache/caps_gb300/autotune.tsv.  A new
-// tuning version (a change of the kernels the choices were timed with)
-// leaves older lines unused; deleting the file forces new timings.
-static const char *kTuneVersion = "caps-tune-2";
+// tuning version (a change of the kernels or axes the choices were made
+// with) leaves older lines unused; deleting the file forces new timings.
+static const char *kTuneVersion = "caps-tune-3";
 
 static std::string tune_cache_path() {
     const char *e = getenv("CAPS_AUTOTUNE_CACHE");
@@ -1015,15 +1076,16 @@ static bool tune_cache_lookup(int n, const caps_options &o, TuneEntry &out) {
     FILE *f = fopen(path.c_str(), "r");
     if (!f) return false;
     char ver[64], dk[256], pat[16];
-    int fn, fform, fslices, fscheme, nrec, chosen;
+    int fn, fform, fslices, fscheme, nrec, chosen, tile, bits, rejected;
     double sec;
     bool found = false;
-    while (fscanf(f, "%63s %255s %d %d %d %d %d %15s %d %lf", ver, dk, &fn, &fform, &fslices, &fscheme, &nrec, pat,
-                  &chosen, &sec) == 10) {
+    while (fscanf(f, "%63s %255s %d %d %d %d %d %15s %d %d %d %d %lf", ver, dk, &fn, &fform, &fslices, &fscheme,
+                  &nrec, pat, &chosen, &tile, &bits, &rejected, &sec) == 13) {
         if (strcmp(ver, kTuneVersion) || dev != dk || fn != n || fform != o.form || fslices != o.slices ||
-            fscheme != o.split_scheme || nrec < 0 || nrec > 3)
+            fscheme != o.split_scheme || nrec < 0 || nrec > 3 || tile < 0 || tile >= DMMA_TILES || bits < 0 ||
+            bits > 55)
             continue;
-        TuneEntry t{n, o.form, o.slices, nrec, {0}, sec, o.split_scheme, chosen, 1};
+        TuneEntry t{n, o.form, o.slices, nrec, {0}, sec, o.split_scheme, chosen, 1, tile, bits, rejected};
         if (strcmp(pat, "-")) memcpy(t.pat, pat, std::min<size_t>(strlen(pat), 7));
         out = t;
         found = true;  // the last matching line wins
@@ -1049,71 +1111,157 @@ static void tune_cache_store(const TuneEntry &t) {
     }
     FILE *f = fopen(path.c_str(), "a");
     if (!f) return;
-    fprintf(f, "%s\t%s\t%d\t%d\t%d\t%d\t%d\t%s\t%d\t%.9g\n", kTuneVersion, dev.c_str(), t.n, t.form, t.slices,
-            t.scheme, t.nrec, t.pat[0] ? t.pat : "-", t.chosen_scheme, t.seconds);
+    fprintf(f, "%s\t%s\t%d\t%d\t%d\t%d\t%d\t%s\t%d\t%d\t%d\t%d\t%.9g\n", kTuneVersion, dev.c_str(), t.n, t.form,
+            t.slices, t.scheme, t.nrec, t.pat[0] ? t.pat : "-", t.chosen_scheme, t.tile, t.bits, t.rejected,
+            t.seconds);
     fclose(f);
 }
+
+static void cfg_from_entry(const TuneEntry &t, ClassCfg &out) {
+    out.n = t.n;
+    out.nrec = t.nrec;
+    memcpy(out.pat, t.pat, sizeof out.pat);
+    out.scheme = t.chosen_scheme;
+    out.tile = t.tile;
+    out.bits = t.bits;
+}
+
+// Synthetic batch and timing state of one tune_size call.
+struct Tuning {
+    int n = 0, T = 0;
+    int64_t nn = 0;
+    double *data = nullptr;  // instance i: A, B, C at data + 3 nn i (+ nn, + 2 nn)
+    double *ref = nullptr;   // the gate's reference products, nn per instance
+    double *err = nullptr;   // tune_error_kernel's four sums
+    std::vector<BatchItem> items;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+
+    ~Tuning() {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        for (double *p : {data, ref, err})
+            if (p) cudaFree(p);
+    }
+
+    void fill(int wide) {
+        fill_uniform_kernel<<<1024, 256>>>(data, 3 * nn * T, 12345 + n, wide);
+    }
+
+    // Plans and runs one candidate: with `ms`, three runs and the best of the
+    // last two; without, one run (its products are what the gate reads).
+    caps_status run(const ClassCfg &c, const caps_options &o, double *ms) {
+        BatchPlan p;
+        p.items = items;
+        caps_status st = plan_batch(p, {c}, o);
+        double t = 1e30;
+        for (int rep = 0; rep < (ms ? 3 : 1) && st == CAPS_OK; rep++) {
+            cudaEventRecord(e0, 0);
+            st = run_plan_direct(p, 0);
+            cudaEventRecord(e1, 0);
+            if (cudaEventSynchronize(e1) != cudaSuccess) st = CAPS_ERR_CUDA;
+            float x = 0;
+            cudaEventElapsedTime(&x, e0, e1);
+            if (rep > 0) t = std::min(t, (double)x);
+        }
+        if (p.buf.ptr) cudaFree(p.buf.ptr);
+        if (ms) *ms = t;
+        return st;
+    }
+
+    // Squared error sum and largest entry error of the batch's products
+    // against `ref`.
+    caps_status errors(double &s2, double &maxerr) {
+        double h[4] = {0, 0, 0, 0};
+        CAPS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof h, 0));
+        tune_error_kernel<<<152 * 4, 256>>>(data + 2 * nn, ref, nn, T, 3 * nn, err);
+        CAPS_CUDA_TRY(cudaGetLastError());
+        CAPS_CUDA_TRY(cudaMemcpy(h, err, sizeof h, cudaMemcpyDeviceToHost));
+        s2 = h[0];
+        maxerr = h[2];
+        return CAPS_OK;
+    }
+
+    // The accuracy gate of an operand-bit cap (see the tuner's comment).
+    caps_status gate(const ClassCfg &base, int bits, const caps_options &o, bool &ok) {
+        if (!ref) CAPS_TRY(dev_malloc((void **)&ref, (size_t)nn * T * sizeof(double)));
+        if (!err) CAPS_TRY(dev_malloc((void **)&err, 4 * sizeof(double)));
+        caps_options oref = o, oplain = o;
+        oref.form = CAPS_FORM_SPLIT;
+        oref.slices = oref.diagonals = 0;
+        oref.split_scheme = CAPS_SPLIT_AUTO;
+        oplain.form = CAPS_FORM_PLAIN;
+        ClassCfg cref{n, 0, {0}, CAPS_SPLIT_AUTO, DMMA_TILE_64x64, 0};
+        ClassCfg cplain = base;
+        cplain.scheme = 0;
+        cplain.bits = 0;
+        cplain.tile = DMMA_TILE_64x64;
+        ClassCfg cand = base;
+        cand.bits = bits;
+        ok = true;
+        caps_status st = CAPS_OK;
+        for (int wide = 0; wide < 2 && ok && st == CAPS_OK; wide++) {
+            fill(wide);
+            st = run(cref, oref, nullptr);
+            for (int i = 0; i < T && st == CAPS_OK; i++)
+                if (cudaMemcpyAsync(ref + nn * i, data + 3 * nn * i + 2 * nn, (size_t)nn * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, 0) != cudaSuccess)
+                    st = CAPS_ERR_CUDA;
+            double ps2 = 0, pmax = 0, cs2 = 0, cmax = 0;
+            if (st == CAPS_OK) st = run(cplain, oplain, nullptr);
+            if (st == CAPS_OK) st = errors(ps2, pmax);
+            if (st == CAPS_OK) st = run(cand, o, nullptr);
+            if (st == CAPS_OK) st = errors(cs2, cmax);
+            ok = cs2 <= ps2 && cmax <= pmax;  // false for a NaN
+        }
+        fill(0);
+        return st;
+    }
+};
 
 static caps_status tune_size(int n, const caps_options &o, ClassCfg &out) {
     for (const TuneEntry &t : g_tune)
         if (t.n == n && t.form == o.form && t.slices == o.slices && t.scheme == o.split_scheme) {
-            out.n = n;
-            out.nrec = t.nrec;
-            memcpy(out.pat, t.pat, sizeof out.pat);
-            out.scheme = t.chosen_scheme;
+            cfg_from_entry(t, out);
             return CAPS_OK;
         }
     {
         TuneEntry cached;
         if (tune_cache_lookup(n, o, cached)) {
             g_tune.push_back(cached);
-            out.n = n;
-            out.nrec = cached.nrec;
-            memcpy(out.pat, cached.pat, sizeof out.pat);
-            out.scheme = cached.chosen_scheme;
+            cfg_from_entry(cached, out);
             return CAPS_OK;
         }
     }
-    int rmax = max_tune_nrec(n, o.form);
-    int T = (int)std::max<int64_t>(1, std::min<int64_t>(32, ((int64_t)1 << 27) / ((int64_t)n * n)));
-    int64_t nn = (int64_t)n * n;
-    double *data = nullptr;
-    CAPS_TRY(dev_malloc((void **)&data, (size_t)3 * nn * T * sizeof(double)));
-    fill_uniform_kernel<<<1024, 256>>>(data, 3 * nn * T, 12345 + n);
-    std::vector<BatchItem> items;
-    for (int i = 0; i < T; i++) items.push_back({n, data + 3 * nn * i, data + 3 * nn * i + nn, data + 3 * nn * i + 2 * nn});
-    ClassCfg best{n, 0, {0}, o.split_scheme};
+    const int rmax = max_tune_nrec(n, o.form);
+    Tuning tu;
+    tu.n = n;
+    tu.nn = (int64_t)n * n;
+    tu.T = (int)std::max<int64_t>(1, std::min<int64_t>(32, ((int64_t)1 << 27) / tu.nn));
+    CAPS_TRY(dev_malloc((void **)&tu.data, (size_t)3 * tu.nn * tu.T * sizeof(double)));
+    tu.fill(0);
+    for (int i = 0; i < tu.T; i++) {
+        double *d = tu.data + 3 * tu.nn * i;
+        tu.items.push_back({n, d, d + tu.nn, d + 2 * tu.nn});
+    }
+    CAPS_CUDA_TRY(cudaEventCreate(&tu.e0));
+    CAPS_CUDA_TRY(cudaEventCreate(&tu.e1));
+    ClassCfg best{n, 0, {0}, o.split_scheme, DMMA_TILE_64x64, 0};
     double best_t = 1e30;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
     caps_status st = CAPS_OK;
-    // split form, scheme left to the library: time both cuts (residues only
-    // where the leaves fit them; otherwise they would run as digits anyway)
+    // axis 1: depth, pattern and (split form, scheme left to the library)
+    // the operand cut; residues only where the leaves fit them, since they
+    // would run as digits otherwise
     const bool both = o.form == CAPS_FORM_SPLIT && o.split_scheme == CAPS_SPLIT_AUTO && o.slices == 0;
     for (int r = 0; r <= rmax && st == CAPS_OK; r++) {
         const int leaf = n >> r;
         for (int sc = 0; sc < (both ? 2 : 1) && st == CAPS_OK; sc++) {
             const int scheme = both ? (sc == 0 ? CAPS_SPLIT_RESIDUES : CAPS_SPLIT_DIGITS) : o.split_scheme;
-            if (both && scheme == CAPS_SPLIT_RESIDUES && (leaf + 15) / 16 * 16 > 2048) continue;
-            for (int variant = 0; variant < (r >= 2 ? 2 : 1); variant++) {
-                ClassCfg c{n, r, {0}, scheme};
+            if (both && scheme == CAPS_SPLIT_RESIDUES && (leaf + 15) / 16 * 16 > RESIDUE_KMAX) continue;
+            for (int variant = 0; variant < (r >= 2 ? 2 : 1) && st == CAPS_OK; variant++) {
+                ClassCfg c{n, r, {0}, scheme, DMMA_TILE_64x64, 0};
                 for (int k = 0; k < r; k++) c.pat[k] = (variant == 1 && k == 0) ? 'd' : 'b';
-                BatchPlan p;
-                p.items = items;
-                st = plan_batch(p, {c}, o);
-                if (st != CAPS_OK) { if (p.buf.ptr) cudaFree(p.buf.ptr); break; }
                 double t = 1e30;
-                for (int rep = 0; rep < 3 && st == CAPS_OK; rep++) {
-                    cudaEventRecord(e0, 0);
-                    st = run_plan_direct(p, 0);
-                    cudaEventRecord(e1, 0);
-                    if (cudaEventSynchronize(e1) != cudaSuccess) st = CAPS_ERR_CUDA;
-                    float ms = 0;
-                    cudaEventElapsedTime(&ms, e0, e1);
-                    if (rep > 0) t = std::min(t, (double)ms);
-                }
-                if (p.buf.ptr) cudaFree(p.buf.ptr);
+                st = tu.run(c, o, &t);
                 if (st == CAPS_OK && t < best_t) {
                     best_t = t;
                     best = c;
@@ -1121,12 +1269,49 @@ static caps_status tune_size(int n, const caps_options &o, ClassCfg &out) {
             }
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaFree(data);
+    // axis 2: the DMMA tile
+    if (o.form == CAPS_FORM_PLAIN)
+        for (int tile : {(int)DMMA_TILE_32x32, (int)DMMA_TILE_128x64}) {
+            if (st != CAPS_OK) break;
+            ClassCfg c = best;
+            c.tile = tile;
+            double t = 1e30;
+            st = tu.run(c, o, &t);
+            if (st == CAPS_OK && t < best_t) {
+                best_t = t;
+                best = c;
+            }
+        }
+    // axis 3: the operand-bit cap of the residues, gated on accuracy
+    int rejected = 0;
+    const int leaf = n >> best.nrec;
+    if (st == CAPS_OK && o.form == CAPS_FORM_SPLIT && best.scheme == CAPS_SPLIT_RESIDUES &&
+        (leaf + 15) / 16 * 16 <= RESIDUE_KMAX) {
+        std::vector<std::pair<double, int>> faster;
+        for (int bits : {52, 48}) {
+            ClassCfg c = best;
+            c.bits = bits;
+            double t = 1e30;
+            st = tu.run(c, o, &t);
+            if (st != CAPS_OK) break;
+            if (t < best_t) faster.push_back({t, bits});
+        }
+        std::sort(faster.begin(), faster.end());
+        for (const auto &fb : faster) {
+            if (st != CAPS_OK) break;
+            bool ok = false;
+            st = tu.gate(best, fb.second, o, ok);
+            if (st == CAPS_OK && ok) {
+                best.bits = fb.second;
+                best_t = fb.first;
+                break;
+            }
+            rejected++;
+        }
+    }
     if (st != CAPS_OK) return st;
-    TuneEntry te{n, o.form, o.slices, best.nrec, {0}, best_t / 1e3 / T, o.split_scheme,
-                 o.form == CAPS_FORM_SPLIT ? best.scheme : 0, 0};
+    TuneEntry te{n, o.form, o.slices, best.nrec, {0}, best_t / 1e3 / tu.T, o.split_scheme,
+                 o.form == CAPS_FORM_SPLIT ? best.scheme : 0, 0, best.tile, best.bits, rejected};
     memcpy(te.pat, best.pat, sizeof te.pat);
     g_tune.push_back(te);
     tune_cache_store(te);
@@ -1519,6 +1704,35 @@ caps_status caps_autotune_entry_ex(int index, int *n, int *form, int *nrec, char
     if (scheme) *scheme = t.chosen_scheme;
     if (from_cache) *from_cache = t.from_cache;
     if (seconds) *seconds = t.seconds;
+    return CAPS_OK;
+}
+
+caps_status caps_autotune_info(int index, caps_tune_info *out) {
+    std::lock_guard<std::recursive_mutex> g(g_mu);
+    if (!out || index < 0 || index >= (int)g_tune.size()) return CAPS_ERR_ARG;
+    const TuneEntry &t = g_tune[index];
+    memset(out, 0, sizeof *out);
+    out->n = t.n;
+    out->form = t.form;
+    out->nrec = t.nrec;
+    memcpy(out->pattern, t.pat, sizeof out->pattern);
+    out->pattern[sizeof out->pattern - 1] = 0;
+    out->scheme = t.chosen_scheme;
+    const int leaf = t.nrec >= 0 && t.nrec < 31 ? t.n >> t.nrec : t.n;
+    if (t.form == CAPS_FORM_PLAIN) {
+        dmma_tile_shape(t.tile, &out->tile_rows, &out->tile_cols);
+    } else if (t.chosen_scheme == CAPS_SPLIT_RESIDUES && (leaf + 15) / 16 * 16 <= RESIDUE_KMAX) {
+        out->tile_rows = 128;
+        out->tile_cols = 256;
+        out->operand_bits = t.bits > 0 ? t.bits : 55;
+        out->moduli = crt_moduli_needed(out->operand_bits, leaf);
+        out->gate_rejected = t.rejected;
+    } else {
+        out->tile_rows = 128;
+        out->tile_cols = 64;
+    }
+    out->from_cache = t.from_cache;
+    out->seconds = t.seconds;
     return CAPS_OK;
 }
 

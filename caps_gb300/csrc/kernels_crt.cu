@@ -7,7 +7,7 @@
 //
 //  1. scale (shared with the digit scheme): per row i of A the exponent
 //     bound E_i and lowest set bit, per column j of B the same; t_a, t_b =
-//     min(bits needed over the launch group, 55);
+//     min(bits needed over the launch group, 55, the cap SplitParams.bits);
 //     A'_ik = round(a_ik 2^(t_a - E_i)), B'_kj = round(b_kj 2^(t_b - E_j)),
 //     |A'| <= 2^t_a, |B'| <= 2^t_b, exact when the data needs <= t bits.
 //  2. resolve: the fewest moduli L whose product M_L exceeds
@@ -174,6 +174,21 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
 
 }  // namespace
 
+int crt_moduli_needed(int bits, int K) {
+    const int Kp = (K + TK - 1) / TK * TK;
+    int kb = 0;
+    while ((1 << kb) < Kp) kb++;
+    const int need = 2 * bits + kb + 1;  // as crt_resolve_kernel: K 2^(ta+tb) < M_L / 2
+    u128 M = 1;
+    for (int L = 1; L <= LMAX; L++) {
+        M *= (u128)MODULI[L - 1];
+        int lg = 0;
+        while ((M >> (lg + 1)) != 0) lg++;
+        if (lg >= need) return L;
+    }
+    return 0;
+}
+
 // ---------------------------------------------------------------- resolve
 // One thread: picks the scheme for the launch group from the scan's results
 // and writes it into the header, where every later kernel of the group reads it.
@@ -184,9 +199,12 @@ __global__ void crt_resolve_kernel(char *__restrict__ ws, Geo g, SplitParams p) 
     resolve_sd(h, p, s, nd);
     h->s_used = s;
     h->nd_used = nd;
-    const int ta = h->bitsA < 55 ? h->bitsA : 55, tb = h->bitsB < 55 ? h->bitsB : 55;
-    int residues = 0, L = 0;
     const bool forced_digits = p.scheme == SCHEME_DIGITS || (p.scheme == SCHEME_AUTO && p.slices > 0);
+    // operand bits: what the data need, at most 55, at most the cap asked for
+    // (a cap only where the residues run: the digit scheme sets its own cut)
+    const int cap = (p.bits > 0 && p.bits < 55 && !forced_digits) ? p.bits : 55;
+    const int ta = h->bitsA < cap ? h->bitsA : cap, tb = h->bitsB < cap ? h->bitsB : cap;
+    int residues = 0, L = 0;
     if (g.residues_ok && !forced_digits) {
         int kb = 0;
         while ((1 << kb) < g.Kp) kb++;

@@ -5,16 +5,20 @@
 //
 // GB300 runs FP64 (DFMA and DMMA alike) at ~1.05 TFLOP/s for the whole GPU,
 // about 1.8 multiply-adds per clock per SM, so this kernel is bound by the
-// DMMA pipe at any sensible tiling; 64x64 tiles with a 16-deep K slab in
-// shared memory keep operand traffic far below what that pipe can consume.
-// One CTA (4 warps, 2x2, 32x32 per warp of m8n8k4 tiles) per 64x64 tile of
-// one leaf of the batch (blockIdx.z).
+// DMMA pipe at any sensible tiling; a 16-deep K slab in shared memory keeps
+// operand traffic far below what that pipe can consume.  Each warp owns a
+// 32 x 32 block of C (4 x 4 m8n8k4 tiles); a CTA is a WM x WN grid of warps,
+// one CTA per (32 WM) x (32 WN) tile of one leaf of the batch (blockIdx.z).
+// Three shapes (caps_dmma_tile): 64 x 64 (2 x 2 warps, the default),
+// 32 x 32 (one warp: four times the CTAs, for small leaves) and 128 x 64
+// (4 x 2 warps: half the B traffic per multiply-add).  The autotuner times
+// them per size.
 #include "common.cuh"
 
 namespace caps {
 
 namespace {
-constexpr int BM = 64, BN = 64, BK = 16, LDS = 72;  // LDS: padded row (banks)
+constexpr int BK = 16;
 
 __device__ __forceinline__ void dmma_8x8x4(double (&d)[2], double a, double b) {
     asm volatile(
@@ -24,12 +28,15 @@ __device__ __forceinline__ void dmma_8x8x4(double (&d)[2], double a, double b) {
 }
 }  // namespace
 
-__global__ void __launch_bounds__(128) dmma_gemm_kernel(const LeafTask *__restrict__ tasks, int m) {
-    __shared__ double As[BK][LDS];  // As[k][i]
-    __shared__ double Bs[BK][LDS];  // Bs[k][j]
+template <int WM, int WN>
+__global__ void __launch_bounds__(32 * WM * WN) dmma_gemm_kernel(const LeafTask *__restrict__ tasks, int m) {
+    constexpr int BM = 32 * WM, BN = 32 * WN, NT = 32 * WM * WN;
+    constexpr int LDA = BM + 8, LDB = BN + 8;  // padded rows (banks)
+    __shared__ double As[BK][LDA];  // As[k][i]
+    __shared__ double Bs[BK][LDB];  // Bs[k][j]
     const LeafTask t = tasks[blockIdx.z];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int wr = warp >> 1, wc = warp & 1;
+    const int wr = warp / WN, wc = warp % WN;
     const int64_t i0 = (int64_t)blockIdx.y * BM, j0 = (int64_t)blockIdx.x * BN;
     const int64_t M = m;
 
@@ -40,18 +47,19 @@ __global__ void __launch_bounds__(128) dmma_gemm_kernel(const LeafTask *__restri
         for (int b = 0; b < 4; b++) acc[a][b][0] = acc[a][b][1] = 0.0;
 
     for (int64_t k0 = 0; k0 < M; k0 += BK) {
-        // A tile: 64 rows x 16 k, column-major source; thread -> (row, k pair)
+        // A tile: BM rows x 16 k from a column-major source; consecutive
+        // threads read consecutive rows of one column
 #pragma unroll
-        for (int p = 0; p < 8; p++) {
-            int row = tid & 63, kk = (tid >> 6) + 2 * p;
-            int64_t gi = i0 + row, gk = k0 + kk;
+        for (int p = 0; p < BM * BK / NT; p++) {
+            const int e = tid + NT * p, row = e % BM, kk = e / BM;
+            const int64_t gi = i0 + row, gk = k0 + kk;
             As[kk][row] = (gi < M && gk < M) ? t.A[gi + gk * M] : 0.0;
         }
-        // B tile: 16 k x 64 cols; thread -> (k, col)
+        // B tile: 16 k x BN columns; consecutive threads read the 16 k of one column
 #pragma unroll
-        for (int p = 0; p < 8; p++) {
-            int kk = tid & 15, col = (tid >> 4) + 8 * p;
-            int64_t gk = k0 + kk, gj = j0 + col;
+        for (int p = 0; p < BN * BK / NT; p++) {
+            const int e = tid + NT * p, kk = e % BK, col = e / BK;
+            const int64_t gk = k0 + kk, gj = j0 + col;
             Bs[kk][col] = (gk < M && gj < M) ? t.B[gk + gj * M] : 0.0;
         }
         __syncthreads();
@@ -75,22 +83,39 @@ __global__ void __launch_bounds__(128) dmma_gemm_kernel(const LeafTask *__restri
         for (int b = 0; b < 4; b++)
 #pragma unroll
             for (int e = 0; e < 2; e++) {
-                int64_t gi = i0 + 32 * wr + 8 * a + (lane >> 2);
-                int64_t gj = j0 + 32 * wc + 8 * b + 2 * (lane & 3) + e;
+                const int64_t gi = i0 + 32 * wr + 8 * a + (lane >> 2);
+                const int64_t gj = j0 + 32 * wc + 8 * b + 2 * (lane & 3) + e;
                 if (gi < M && gj < M) t.C[gi + gj * M] = acc[a][b][e];
             }
 }
 
-cudaError_t launch_dmma_gemm(const LeafTask *tasks_dev, int count, int m, cudaStream_t stream) {
-    if (count <= 0 || m <= 0) return cudaSuccess;
-    unsigned tiles = (unsigned)((m + BM - 1) / BM);
+template <int WM, int WN>
+static cudaError_t launch_dmma_shape(const LeafTask *tasks_dev, int count, int m, cudaStream_t stream) {
+    const unsigned rows = (unsigned)((m + 32 * WM - 1) / (32 * WM)), cols = (unsigned)((m + 32 * WN - 1) / (32 * WN));
     for (int base = 0; base < count; base += 65535) {
-        int c = count - base < 65535 ? count - base : 65535;
-        dim3 grid(tiles, tiles, (unsigned)c);
-        dmma_gemm_kernel<<<grid, 128, 0, stream>>>(tasks_dev + base, m);
+        const int c = count - base < 65535 ? count - base : 65535;
+        dim3 grid(cols, rows, (unsigned)c);
+        dmma_gemm_kernel<WM, WN><<<grid, 32 * WM * WN, 0, stream>>>(tasks_dev + base, m);
         count_launch();
     }
     return cudaGetLastError();
+}
+
+void dmma_tile_shape(int tile, int *rows, int *cols) {
+    switch (tile) {
+        case DMMA_TILE_32x32: *rows = 32; *cols = 32; break;
+        case DMMA_TILE_128x64: *rows = 128; *cols = 64; break;
+        default: *rows = 64; *cols = 64; break;
+    }
+}
+
+cudaError_t launch_dmma_gemm(const LeafTask *tasks_dev, int count, int m, cudaStream_t stream, int tile) {
+    if (count <= 0 || m <= 0) return cudaSuccess;
+    switch (tile) {
+        case DMMA_TILE_32x32: return launch_dmma_shape<1, 1>(tasks_dev, count, m, stream);
+        case DMMA_TILE_128x64: return launch_dmma_shape<4, 2>(tasks_dev, count, m, stream);
+        default: return launch_dmma_shape<2, 2>(tasks_dev, count, m, stream);
+    }
 }
 
 }  // namespace caps

@@ -102,7 +102,7 @@ extern "C" caps_status caps_leaf_gemm_split_noalloc_dev(const double *A, const d
     caps::LeafTask *task = reinterpret_cast<caps::LeafTask *>(ws + TASK_OFF);
     unsigned *status = reinterpret_cast<unsigned *>(ws + STATUS_OFF);
     cudaStream_t s = (cudaStream_t)stream;
-    caps::SplitParams p;
+    caps::SplitParams p{};
     p.slices = slices;
     p.diagonals = diagonals;
     p.scheme = CAPS_SPLIT_DIGITS;  // the scratch array is sized for digit planes

@@ -75,8 +75,19 @@ typedef struct caps_options {
     int diagonals;             /* split form: digit-pair diagonals kept, 0 = automatic */
     int split_scheme;          /* split form: caps_split_scheme */
     long long workspace_limit; /* bytes of device workspace allowed (-m); <= 0: no limit */
-    long long reserved[4];
+    int plain_tile;            /* plain form: the DMMA base case's CTA tile, caps_plain_tile */
+    int operand_bits;          /* split form, residue scheme: cap on the operand bits, 0 = 55
+                                  (the data's own need when lower); fewer bits take fewer moduli
+                                  and round the operands more coarsely.  1..55 */
+    long long reserved[3];
 } caps_options;
+
+/* CTA tiles of the plain form's DMMA base case. */
+typedef enum caps_plain_tile {
+    CAPS_TILE_64x64 = 0,   /* default */
+    CAPS_TILE_32x32 = 1,   /* one warp per CTA: four times the CTAs, for small leaves */
+    CAPS_TILE_128x64 = 2   /* eight warps: half the B traffic per multiply-add */
+} caps_plain_tile;
 
 /* Fills *opt with defaults (plain form, automatic slices, no limit). */
 void caps_options_init(caps_options *opt);
@@ -214,10 +225,40 @@ caps_status caps_autotune_entry(int index, int *n, int *form, int *nrec, char *p
  * with an automatic scheme, residues against digits.  Its choices are kept
  * in CAPS_AUTOTUNE_CACHE (a file; empty: no cache) or by default in
  * $HOME/.cache/caps_gb300/autotune.tsv, keyed by the device's name and SM
- * count, the size, form, slices and asked-for scheme.  Tile shapes are fixed
- * per kernel.  Any pointer may be NULL. */
+ * count, the size, form, slices and asked-for scheme.  Any pointer may be
+ * NULL.  caps_autotune_info gives every axis. */
 caps_status caps_autotune_entry_ex(int index, int *n, int *form, int *nrec, char *pattern, int *scheme,
                                    int *from_cache, double *seconds);
+
+/* One autotuner choice with all its axes. */
+typedef struct {
+    int n;              /* matrix size */
+    int form;           /* caps_form */
+    int nrec;           /* Strassen levels */
+    char pattern[8];    /* b/d per level, NUL-terminated */
+    int scheme;         /* split form: the scheme chosen (caps_split_scheme); plain form: 0 */
+    int tile_rows;      /* CTA tile of the base-case GEMM: plain form 64 x 64, 32 x 32 or */
+    int tile_cols;      /*   128 x 64 (searched); residues 128 x 256, digits 128 x 64 (fixed) */
+    int operand_bits;   /* residues: operand bits per entry (55, or a smaller cap that won); else 0 */
+    int moduli;         /* residues: moduli per leaf product for float data at that cap; else 0 */
+    int gate_rejected;  /* residues: smaller bit caps that ran faster but failed the accuracy gate */
+    int from_cache;     /* 1: read from the on-disk cache */
+    double seconds;     /* per instance, of the choice */
+} caps_tune_info;
+
+/* Autotuner choice `index` (0, 1, ...) with all its axes; CAPS_ERR_ARG past
+ * the last entry or for a NULL `out`.  The tuner searches, in turn:
+ *   1. recursion depth (0..3 as the leaves allow) and the top step's b/d
+ *      pattern, and for the split form with an automatic scheme, residues
+ *      against digits;
+ *   2. plain form: the DMMA tile;
+ *   3. split form where the residues won: operand bits 55 / 52 / 48 (17 / 16 /
+ *      15 moduli at K <= 2048), a smaller cap kept only if it is faster and
+ *      its error against a split reference is no larger than the plain FP64
+ *      form's at the same depth and pattern (normwise and largest entry), on
+ *      uniform and on wide-range (u 2^k, |k| <= 20) synthetic inputs.
+ * No reference counterpart. */
+caps_status caps_autotune_info(int index, caps_tune_info *out);
 
 /* Human-readable text of a status. */
 const char *caps_status_string(caps_status s);

@@ -618,13 +618,17 @@ static int residue_scales(int64_t m, const double *X, int side, int *E)
     return bits;
 }
 
-void caps_oracle_split_gemm_residues(int64_t m, const double *A, const double *B, double *C, int *t_out)
+/* The same with the operand bits capped at `cap` (1..55) instead of 55:
+ * t_a = min(bits the rows need, cap), likewise t_b. */
+void caps_oracle_split_gemm_residues_bits(int64_t m, const double *A, const double *B, double *C, int *t_out,
+                                          int cap)
 {
     int *Ea = (int *)malloc((size_t)m * sizeof(int));
     int *Eb = (int *)malloc((size_t)m * sizeof(int));
     int ta = residue_scales(m, A, 0, Ea), tb = residue_scales(m, B, 1, Eb);
-    if (ta > 55) ta = 55;
-    if (tb > 55) tb = 55;
+    if (cap < 1 || cap > 55) cap = 55;
+    if (ta > cap) ta = cap;
+    if (tb > cap) tb = cap;
     if (t_out) { t_out[0] = ta; t_out[1] = tb; }
     int64_t *X = (int64_t *)malloc((size_t)(m * m) * sizeof(int64_t));  /* row-major X[i][k] */
     int64_t *Y = (int64_t *)malloc((size_t)(m * m) * sizeof(int64_t));  /* Y[j][k] */
@@ -647,4 +651,9 @@ void caps_oracle_split_gemm_residues(int64_t m, const double *A, const double *B
         }
     }
     free(X); free(Y); free(Ea); free(Eb);
+}
+
+void caps_oracle_split_gemm_residues(int64_t m, const double *A, const double *B, double *C, int *t_out)
+{
+    caps_oracle_split_gemm_residues_bits(m, A, B, C, t_out, 55);
 }

@@ -92,6 +92,9 @@ def lib():
         L.caps_oracle_set_dgemm.restype = None
         L.caps_oracle_split_gemm_residues.restype = None
         L.caps_oracle_split_gemm_residues.argtypes = [ctypes.c_int64, _dp, _dp, _dp, ctypes.POINTER(ctypes.c_int)]
+        L.caps_oracle_split_gemm_residues_bits.restype = None
+        L.caps_oracle_split_gemm_residues_bits.argtypes = [ctypes.c_int64, _dp, _dp, _dp, ctypes.POINTER(ctypes.c_int),
+                                                           ctypes.c_int]
         L.caps_oracle_set_dgemm.argtypes = [ctypes.c_void_p]
         L.caps_oracle_set_threads.restype = None
         L.caps_oracle_set_threads.argtypes = [ctypes.c_int]
@@ -241,14 +244,15 @@ def split_gemm(A_cm: np.ndarray, B_cm: np.ndarray, m: int, s: int, nd: int) -> n
     return C
 
 
-def split_gemm_residues(A_cm: np.ndarray, B_cm: np.ndarray, m: int):
+def split_gemm_residues(A_cm: np.ndarray, B_cm: np.ndarray, m: int, bits: int = 55):
     """Exact CPU model of the residue scheme's leaf product (column-major):
     the 128-bit integer product of the scaled operands, rounded once.
+    bits: cap on the operand bits (55 unless the tuner or caller asks fewer).
     Returns (C, (t_a, t_b))."""
     C = np.empty(m * m, dtype=np.float64)
     t = (ctypes.c_int * 2)()
-    lib().caps_oracle_split_gemm_residues(m, _p(np.ascontiguousarray(A_cm)), _p(np.ascontiguousarray(B_cm)),
-                                          _p(C), t)
+    lib().caps_oracle_split_gemm_residues_bits(m, _p(np.ascontiguousarray(A_cm)), _p(np.ascontiguousarray(B_cm)),
+                                               _p(C), t, int(bits))
     return C, (t[0], t[1])
 
 

@@ -15,14 +15,14 @@ def mat_of(oracle, flat, n, r, bs=1):
 
 
 def gpu_multiply(caps, oracle, A, B, r, bs=1, pattern=None, form="plain", slices=0, diagonals=0,
-                 device="cuda:0", scheme="auto"):
+                 device="cuda:0", scheme="auto", tile=0, operand_bits=0):
     import torch
     n = A.shape[0]
     dA = torch.from_numpy(caps_of(oracle, A, r, bs)).to(device)
     dB = torch.from_numpy(caps_of(oracle, B, r, bs)).to(device)
     dC = torch.full_like(dA, float("nan"))
     caps.multiply(dA, dB, dC, caps.MatDescriptor.make(n, r, bs), pattern, form=form, slices=slices,
-                  diagonals=diagonals, scheme=scheme)
+                  diagonals=diagonals, scheme=scheme, tile=tile, operand_bits=operand_bits)
     torch.cuda.synchronize()
     return mat_of(oracle, dC.cpu().numpy(), n, r, bs)
 

@@ -98,5 +98,54 @@ def test_autotune_choices_persist_on_disk(caps, cuda, tmp_path):
     assert set(first) == set(second) == {448, 224}
     for n in first:
         assert not first[n]["from_cache"] and second[n]["from_cache"]
-        for k in ("nrec", "pattern", "scheme"):
+        for k in ("nrec", "pattern", "scheme", "tile", "operand_bits", "moduli"):
             assert first[n][k] == second[n][k], (n, k)
+
+
+def _sampled_errors(oracle_mod, C_cm, A_cm, B_cm, n, seed):
+    rng = np.random.default_rng(seed)
+    rows, cols = rng.integers(0, n, 256), rng.integers(0, n, 256)
+    hi, lo = oracle_mod.dd_entries(A_cm, B_cm, n, rows, cols)
+    ab = oracle_mod.absprod_entries(A_cm, B_cm, n, rows, cols)
+    m = oracle_mod.error_metrics(C_cm.reshape(n, n)[cols, rows], hi, lo, ab)
+    return m["max_elementwise_rel"], m["normwise_rel"]
+
+
+def test_autotuner_axes_and_split_no_worse_than_plain(caps, cuda, oracle_mod):
+    """The tuner's table carries every axis (depth, pattern, scheme, tile,
+    operand bits / moduli); whatever it chose, the batched split products are
+    no less accurate than the batched plain FP64 ones, on uniform and on
+    wide-range inputs (the promise its accuracy gate on the bit cap keeps)."""
+    import torch
+    sizes = [1792, 448, 1792]
+    rng = np.random.default_rng(21)
+    for wide in (False, True):
+        As, Bs, host = [], [], []
+        for n in sizes:
+            A = rng.uniform(-1, 1, n * n)
+            B = rng.uniform(-1, 1, n * n)
+            if wide:
+                A *= 2.0 ** rng.integers(-20, 21, n * n)
+                B *= 2.0 ** rng.integers(-20, 21, n * n)
+            host.append((A, B))
+            As.append(torch.from_numpy(A).to(cuda))
+            Bs.append(torch.from_numpy(B).to(cuda))
+        err = {}
+        for form in ("split", "plain"):
+            Cs = [torch.full((n * n,), float("nan"), dtype=torch.float64, device=cuda) for n in sizes]
+            caps.multiply_batched(As, Bs, Cs, sizes, form=form)
+            torch.cuda.synchronize()
+            err[form] = [_sampled_errors(oracle_mod, C.cpu().numpy(), A, B, n, 5 + i)
+                         for i, ((A, B), C, n) in enumerate(zip(host, Cs, sizes))]
+        for (ew_s, nw_s), (ew_p, nw_p), n in zip(err["split"], err["plain"], sizes):
+            assert ew_s <= ew_p and nw_s <= nw_p, (wide, n, ew_s, ew_p, nw_s, nw_p)
+    tab = {(t["n"], t["form"]): t for t in caps.autotune_table()}
+    for n in (448, 1792):
+        p = tab[(n, "plain")]
+        assert p["tile"] in ([64, 64], [32, 32], [128, 64]) and p["operand_bits"] == 0 and p["scheme"] is None
+        s = tab[(n, "split")]
+        if s["scheme"] == "residues" and (n >> s["nrec"]) <= 2048:
+            assert s["tile"] == [128, 256] and s["operand_bits"] in (55, 52, 48)
+            assert s["moduli"] == {55: 17, 52: 16, 48: 15}[s["operand_bits"]]  # K of 448..2048
+        else:
+            assert s["tile"] == [128, 64] and s["operand_bits"] == 0 and s["moduli"] == 0

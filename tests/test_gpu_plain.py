@@ -64,6 +64,51 @@ def test_dmma_leaf_gemm(caps, oracle_mod, cuda, m):
     assert ew <= m * 2.0 ** -53
 
 
+@pytest.mark.parametrize("tile", ["32x32", "128x64"])
+@pytest.mark.parametrize("m", [1, 20, 33, 100, 130, 515])
+def test_dmma_leaf_tiles_bitidentical_to_default(caps, oracle_mod, cuda, m, tile):
+    """The three DMMA tile shapes (an autotuner axis) accumulate every entry
+    over k in the same order, so on float data they agree bit for bit; on
+    integers they equal the exact product."""
+    import torch
+    rng = np.random.default_rng(3 * m)
+    Af = torch.from_numpy(rng.uniform(-1, 1, m * m)).to(cuda)
+    Bf = torch.from_numpy(rng.uniform(-1, 1, m * m)).to(cuda)
+    C0 = torch.full_like(Af, float("nan"))
+    C1 = torch.full_like(Af, float("nan"))
+    caps.leaf_gemm(Af, Bf, C0, m)
+    caps.leaf_gemm(Af, Bf, C1, m, tile=tile)
+    torch.cuda.synchronize()
+    assert torch.equal(C0, C1)
+    Ai = rng.integers(-50, 51, (m, m)).astype(np.float64)
+    Bi = rng.integers(-50, 51, (m, m)).astype(np.float64)
+    caps.leaf_gemm(torch.from_numpy(Ai.T.copy().reshape(-1)).to(cuda),
+                   torch.from_numpy(Bi.T.copy().reshape(-1)).to(cuda), C1, m, tile=tile)
+    torch.cuda.synchronize()
+    got = C1.cpu().numpy().reshape(m, m).T
+    assert np.array_equal(got, (Ai.astype(np.int64) @ Bi.astype(np.int64)).astype(np.float64))
+
+
+@pytest.mark.parametrize("tile", ["32x32", "128x64"])
+def test_plain_multiply_tiles_on_reference_fixtures(caps, oracle_mod, ref_tests, cuda, tile):
+    """Whole plain multiplies with a non-default tile on the reference's
+    integer fixtures (n = 196 and 392, 'd' and 'b' steps): deviation 0; and on
+    floats bit-identical to the default tile."""
+    for n in (196, 392):
+        A = ref_tests["A%d" % n].astype(np.float64)
+        B = ref_tests["B%d" % n].astype(np.float64)
+        exact = (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64)
+        for bs, r in ref_tests["params%d" % n]:
+            for pat in ("d" * r, "b" * r):
+                C = gpu_multiply(caps, oracle_mod, A, B, r, bs, pat, tile=tile)
+                assert np.array_equal(C, exact), (n, bs, r, pat)
+    rng = np.random.default_rng(11)
+    Af, Bf = rng.uniform(-1, 1, (512, 512)), rng.uniform(-1, 1, (512, 512))
+    C0 = gpu_multiply(caps, oracle_mod, Af, Bf, 2, 1, "bd")
+    C1 = gpu_multiply(caps, oracle_mod, Af, Bf, 2, 1, "bd", tile=tile)
+    assert np.array_equal(C0, C1)
+
+
 @pytest.mark.parametrize("n", [28, 42, 56, 196, 294, 392])
 def test_reference_known_answers_plain(caps, oracle_mod, ref_tests, cuda, n):
     """The reference's integer fixtures, every one-rank (-b, -r), 'd' and 'b' steps: deviation 0."""

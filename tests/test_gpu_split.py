@@ -14,13 +14,13 @@ from helpers import caps_of, mat_of, gpu_multiply, dd_of, rel_err
 pytestmark = pytest.mark.gpu
 
 
-def _leaf(caps, cuda, A, B, s=0, nd=0, scheme="auto"):
+def _leaf(caps, cuda, A, B, s=0, nd=0, scheme="auto", operand_bits=0):
     import torch
     m = A.shape[0]
     C = torch.full((m * m,), float("nan"), dtype=torch.float64, device=cuda)
     caps.leaf_gemm(torch.from_numpy(A.T.copy().reshape(-1)).to(cuda),
                    torch.from_numpy(B.T.copy().reshape(-1)).to(cuda), C, m, form="split", slices=s, diagonals=nd,
-                   scheme=scheme)
+                   scheme=scheme, operand_bits=operand_bits)
     torch.cuda.synchronize()
     return C.cpu().numpy().reshape(m, m).T, caps.counters()
 
@@ -138,10 +138,33 @@ def expected_moduli(ta, tb, m):
     return None
 
 
-def _residue_ref(oracle_mod, A, B):
+def _residue_ref(oracle_mod, A, B, bits=55):
     m = A.shape[0]
-    ref, t = oracle_mod.split_gemm_residues(A.T.copy().reshape(-1), B.T.copy().reshape(-1), m)
+    ref, t = oracle_mod.split_gemm_residues(A.T.copy().reshape(-1), B.T.copy().reshape(-1), m, bits)
     return ref.reshape(m, m).T, t
+
+
+@pytest.mark.parametrize("bits", [52, 48, 30])
+@pytest.mark.parametrize("m,wide", [(512, False), (200, True), (2048, False)])
+def test_residue_leaf_operand_bit_cap_bitexact_vs_model(caps, oracle_mod, cuda, m, wide, bits):
+    """A cap on the operand bits (the autotuner's modulus-count axis) takes
+    fewer moduli and still equals the oracle's 128-bit model at that cap."""
+    rng = np.random.default_rng(7 * m + bits)
+    A = rng.uniform(-1, 1, (m, m))
+    B = rng.uniform(-1, 1, (m, m))
+    if wide:
+        A *= 2.0 ** rng.integers(-20, 21, (m, m))
+        B *= 2.0 ** rng.integers(-20, 21, (m, m))
+    C, cnt = _leaf(caps, cuda, A, B, scheme="residues", operand_bits=bits)
+    ref, (ta, tb) = _residue_ref(oracle_mod, A, B, bits)
+    assert ta == tb == bits
+    assert cnt["split_moduli"] == expected_moduli(bits, bits, m) < expected_moduli(55, 55, m)
+    assert np.array_equal(C, ref)
+    # integer data needing fewer bits than the cap stay exact
+    Ai = rng.integers(-1024, 1025, (m, m)).astype(np.float64)
+    Bi = rng.integers(-1024, 1025, (m, m)).astype(np.float64)
+    C, _ = _leaf(caps, cuda, Ai, Bi, scheme="residues", operand_bits=bits)
+    assert np.array_equal(C, (Ai.astype(np.int64) @ Bi.astype(np.int64)).astype(np.float64))
 
 
 @pytest.mark.parametrize("m", [128, 64, 14, 200, 512, 1100, 2048])

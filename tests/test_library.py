@@ -182,3 +182,39 @@ def test_chol_mult_validation_before_any_device_work(caps):
     buf = (ctypes.c_double * 4)()
     hp = ctypes.cast(buf, dp)
     assert L.caps_chol_mult_host(hp, hp, hp, 0, 1, 0, 1.0, None, ctypes.byref(opt)) == 2
+
+
+def test_struct_layouts_match_header(caps, tmp_path):
+    """caps_options and caps_tune_info as a C compiler lays them out equal the
+    ctypes mirrors (sizes and every field offset)."""
+    structs = {"caps_options": caps.Options, "caps_tune_info": caps.TuneInfo}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "caps_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for field, _ in py._fields_:
+            lines.append(f'printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], stdout=subprocess.PIPE, text=True, check=True).stdout.split("\n")
+    got = {(a, b): int(c) for a, b, c in (ln.split() for ln in out if ln)}
+    for cname, py in structs.items():
+        assert got[(cname, "sizeof")] == ctypes.sizeof(py), cname
+        for field, _ in py._fields_:
+            assert got[(cname, field)] == getattr(py, field).offset, (cname, field)
+
+
+def test_tile_and_operand_bits_validated(caps):
+    L = caps.lib()
+    d = caps.MatDescriptor.make(512, 1)
+    out = ctypes.c_longlong()
+    for kw, status in (({"tile": 2}, 0), ({"tile": "32x32"}, 0), ({"tile": 3}, 8), ({"tile": -1}, 8),
+                       ({"operand_bits": 48}, 0), ({"operand_bits": 55}, 0), ({"operand_bits": 56}, 8),
+                       ({"operand_bits": -1}, 8)):
+        opt = caps.options("split", **kw)
+        assert L.caps_workspace_size(d, b"b", ctypes.byref(opt), ctypes.byref(out)) == status, kw
+    # the tuner's table is empty before any batched call
+    assert caps.autotune_table() == []
+    assert L.caps_autotune_info(0, None) == 8
