@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--slices", type=int, default=0)
     ap.add_argument("--scheme", default="auto", choices=["auto", "digits", "residues"],
                     help="split-form operand cut (auto: from the data)")
+    ap.add_argument("--operand-bits", type=int, default=-1,
+                    help="residue operand-bit cap: -1 = the library's accuracy-gated choice per leaf size "
+                         "(55, 52 or 48), 0 = 55, else 1..55")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-wide", action="store_true", help="skip the wide-range (u*2^k) error check")
@@ -635,7 +638,7 @@ def main():
 
     def step(form, c=C):
         cg.multiply(A, B, c, desc, pattern, form=form, slices=args.slices, stream=stream.cuda_stream,
-                    scheme=args.scheme)
+                    scheme=args.scheme, operand_bits=args.operand_bits)
 
     # ---- headline: split form, device resident
     for _ in range(max(args.warmup, 3)):
@@ -690,6 +693,16 @@ def main():
                          "read + written / their kernels' CUDA-event time)"},
         "hbm_copy_gbs": hbm_peak}
     s_used, nd_used, moduli = cnt["split_slices"], cnt["split_diagonals"], cnt["split_moduli"]
+    # the operand bits the residues ran with, and how they were chosen
+    leaf_gate = [t for t in cg.autotune_table() if t["leaf_gate"] and t["n"] == n >> r]
+    if args.operand_bits < 0:
+        bits_used = leaf_gate[-1]["operand_bits"] if leaf_gate else 55
+        bits_how = ("library's choice for leaves of %d: the fewest bits among 55/52/48 that ran faster and "
+                    "whose leaf product was no less accurate than the FP64 DMMA leaf's on uniform and "
+                    "wide-range inputs (%d faster cap(s) rejected)"
+                    % (n >> r, leaf_gate[-1]["gate_rejected"] if leaf_gate else 0))
+    else:
+        bits_used, bits_how = (args.operand_bits or 55), "fixed by --operand-bits"
     value = replica_throughput(2.0 * n ** 3 / 1e12, world, t_split)
 
     # ---- e2e through the host entry point (pinned host buffers).  Timed
@@ -701,13 +714,15 @@ def main():
     # the call a user makes: no pattern, the library's choice for host arrays
     # (a top-level 'd' step whose subproducts overlap the copies)
     e2e_pattern = cg.resolve_pattern(desc, None, form="split", workspace_limit=96 << 30)
-    cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices, scheme=args.scheme)
+    cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices, scheme=args.scheme,
+                    operand_bits=args.operand_bits)
     barrier(world)
     e2e_steps = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
         ts = time.perf_counter()
-        cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices, scheme=args.scheme)
+        cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices, scheme=args.scheme,
+                    operand_bits=args.operand_bits)
         e2e_steps.append((time.perf_counter() - ts) * 1e3)
     t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
     # the copy rates again: on a shared host they can drop while the leg runs
@@ -715,7 +730,8 @@ def main():
     # one more call with timing events on the copy stream: where its time goes
     cg.set_phase_timing(True)
     ts = time.perf_counter()
-    cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices, scheme=args.scheme)
+    cg.multiply(nA, nB, nC, desc, None, form="split", slices=args.slices, scheme=args.scheme,
+                    operand_bits=args.operand_bits)
     tl_wall = (time.perf_counter() - ts) * 1e3
     cg.set_phase_timing(False)
     tc = cg.counters()
@@ -767,7 +783,7 @@ def main():
             wide = {}
             for form in (("split",) if args.no_plain else ("split", "plain")):
                 cg.multiply(Aw, Bw, Cw, desc, pattern, form=form, slices=args.slices, stream=stream.cuda_stream,
-                            scheme=args.scheme)
+                            scheme=args.scheme, operand_bits=args.operand_bits)
                 torch.cuda.synchronize()
                 wide[form] = sampled_error(colmajor(Cw), Aw_cm, Bw_cm, n, args.samples)
                 if form == "split":
@@ -807,6 +823,7 @@ def main():
                            n, r, "residues modulo %d moduli" % moduli if moduli else "%d digits" % s_used),
                        "n": n, "nrec": r, "pattern": pattern, "form": "split",
                        "scheme": "residues" if moduli else "digits", "moduli": moduli, "slices": s_used,
+                       "operand_bits": bits_used if moduli else None, "operand_bits_choice": bits_how,
                        "diagonals": nd_used, "digit_pairs": pairs,
                        "inputs": "float64 uniform[-1,1) seeded (torch.Generator), CAPS layout",
                        "l2": "inputs larger than L2 (each matrix 2 GiB vs 129 MB L2)",

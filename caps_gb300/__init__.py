@@ -71,7 +71,7 @@ class TuneInfo(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int), ("form", ctypes.c_int), ("nrec", ctypes.c_int), ("pattern", ctypes.c_char * 8),
                 ("scheme", ctypes.c_int), ("tile_rows", ctypes.c_int), ("tile_cols", ctypes.c_int),
                 ("operand_bits", ctypes.c_int), ("moduli", ctypes.c_int), ("gate_rejected", ctypes.c_int),
-                ("from_cache", ctypes.c_int), ("seconds", ctypes.c_double)]
+                ("leaf_gate", ctypes.c_int), ("from_cache", ctypes.c_int), ("seconds", ctypes.c_double)]
 
 
 class Options(ctypes.Structure):
@@ -180,7 +180,8 @@ def options(form: int | str = CAPS_FORM_PLAIN, slices: int = 0, diagonals: int =
             workspace_limit: int = 0, scheme: int | str = 0, tile: int | str = 0,
             operand_bits: int = 0) -> Options:
     """caps_options.  tile: the plain form's DMMA tile ("64x64", "32x32",
-    "128x64"); operand_bits: the residue scheme's operand-bit cap (0 = 55)."""
+    "128x64"); operand_bits: the residue scheme's operand-bit cap (0 = 55; -1:
+    chosen by the library per leaf size under its accuracy gate)."""
     if isinstance(form, str):
         form = {"plain": CAPS_FORM_PLAIN, "split": CAPS_FORM_SPLIT}[form]
     if isinstance(scheme, str):
@@ -322,7 +323,8 @@ def autotune_table() -> list:
         out.append({"n": t.n, "form": "split" if t.form == 1 else "plain", "nrec": t.nrec,
                     "pattern": t.pattern.decode(), "scheme": names.get(t.scheme, t.scheme),
                     "tile": [t.tile_rows, t.tile_cols], "operand_bits": t.operand_bits, "moduli": t.moduli,
-                    "gate_rejected": t.gate_rejected, "from_cache": bool(t.from_cache),
+                    "gate_rejected": t.gate_rejected, "leaf_gate": bool(t.leaf_gate),
+                    "from_cache": bool(t.from_cache),
                     "seconds_per_instance": t.seconds})
         i += 1
 

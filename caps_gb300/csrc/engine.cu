@@ -509,7 +509,7 @@ static caps_status check_opts(const caps_options &o) {
     if (o.diagonals < 0 || o.diagonals > 8) return CAPS_ERR_ARG;
     if (o.split_scheme < CAPS_SPLIT_AUTO || o.split_scheme > CAPS_SPLIT_RESIDUES) return CAPS_ERR_ARG;
     if (o.plain_tile < CAPS_TILE_64x64 || o.plain_tile > CAPS_TILE_128x64) return CAPS_ERR_ARG;
-    if (o.operand_bits < 0 || o.operand_bits > 55) return CAPS_ERR_ARG;
+    if (o.operand_bits < CAPS_OPERAND_BITS_TUNED || o.operand_bits > 55) return CAPS_ERR_ARG;
     return CAPS_OK;
 }
 
@@ -767,12 +767,16 @@ static caps_status check_device_status(cudaStream_t s, const void *last_split_ws
     return CAPS_OK;
 }
 
+static caps_status resolve_operand_bits(const caps_desc &d, caps_options &o);
+
 static caps_status multiply_dev_locked(const double *A, const double *B, double *C, caps_desc d,
-                                       const char *pattern, const caps_options &o, cudaStream_t s,
+                                       const char *pattern, const caps_options &o_in, cudaStream_t s,
                                        bool sync_status, bool host_overlap = false) {
     CAPS_TRY(check_desc(d));
     CAPS_TRY(check_pattern(d, pattern));
-    CAPS_TRY(check_opts(o));
+    CAPS_TRY(check_opts(o_in));
+    caps_options o = o_in;
+    CAPS_TRY(resolve_operand_bits(d, o));
     if (!A || !B || !C) return CAPS_ERR_ARG;
     char pat[32];
     if (pattern) {
@@ -817,10 +821,11 @@ static caps_status multiply_dev_locked(const double *A, const double *B, double 
 
 // ------------------------------------------------------------------ batched
 // Independent multiplies of uneven sizes (column-major in and out).  The
-// instances are grouped by size; for each size the autotuner picks the depth
-// and b/d pattern; inputs are reordered to CAPS layout on the device, every
-// instance of a size class runs in one batched recursion (its base case one
-// persistent GEMM launch per launch group), and results are reordered back.
+// instances are grouped by size; for each size the autotuner picks the depth,
+// b/d pattern, split scheme, DMMA tile and residue operand bits; inputs are
+// reordered to CAPS layout on the device, every instance of a size class
+// runs in one batched recursion (its base case one persistent GEMM launch per
+// launch group), and results are reordered back.
 // The whole sequence is captured once as a CUDA graph and replayed while the
 // same batch (sizes and pointers) comes back.
 
@@ -1218,21 +1223,31 @@ struct Tuning {
     }
 };
 
-static caps_status tune_size(int n, const caps_options &o, ClassCfg &out) {
+// Choices made for single multiplies' leaves (bits_only) are kept under the
+// asked-for scheme plus this offset, apart from the batched classes' ones.
+constexpr int kLeafGateKey = 8;
+
+// bits_only: the operand-bit cap alone, for leaves of n run at depth 0 with
+// residues (a single multiply's leaves with operand_bits = -1).
+static caps_status tune_size(int n, const caps_options &o_in, ClassCfg &out, bool bits_only = false) {
+    caps_options o = o_in;
+    if (bits_only) o.split_scheme = CAPS_SPLIT_RESIDUES;
+    caps_options key = o_in;  // what the choice is kept under
+    if (bits_only) key.split_scheme += kLeafGateKey;
     for (const TuneEntry &t : g_tune)
-        if (t.n == n && t.form == o.form && t.slices == o.slices && t.scheme == o.split_scheme) {
+        if (t.n == n && t.form == key.form && t.slices == key.slices && t.scheme == key.split_scheme) {
             cfg_from_entry(t, out);
             return CAPS_OK;
         }
     {
         TuneEntry cached;
-        if (tune_cache_lookup(n, o, cached)) {
+        if (tune_cache_lookup(n, key, cached)) {
             g_tune.push_back(cached);
             cfg_from_entry(cached, out);
             return CAPS_OK;
         }
     }
-    const int rmax = max_tune_nrec(n, o.form);
+    const int rmax = bits_only ? 0 : max_tune_nrec(n, o.form);
     Tuning tu;
     tu.n = n;
     tu.nn = (int64_t)n * n;
@@ -1310,12 +1325,31 @@ static caps_status tune_size(int n, const caps_options &o, ClassCfg &out) {
         }
     }
     if (st != CAPS_OK) return st;
-    TuneEntry te{n, o.form, o.slices, best.nrec, {0}, best_t / 1e3 / tu.T, o.split_scheme,
+    TuneEntry te{n, o.form, o.slices, best.nrec, {0}, best_t / 1e3 / tu.T, key.split_scheme,
                  o.form == CAPS_FORM_SPLIT ? best.scheme : 0, 0, best.tile, best.bits, rejected};
     memcpy(te.pat, best.pat, sizeof te.pat);
     g_tune.push_back(te);
     tune_cache_store(te);
     out = best;
+    return CAPS_OK;
+}
+
+// caps_options.operand_bits = -1: the residue scheme's operand-bit cap for
+// this multiply's leaves, chosen once per leaf size and kept with the
+// autotuner's choices (tune_size, bits_only): 55 bits, or 52 / 48 where they
+// are faster and pass the accuracy gate against the FP64 DMMA leaf.  Leaves
+// the residues do not run (digits forced, slices given, K above 2048) get 0.
+static caps_status resolve_operand_bits(const caps_desc &d, caps_options &o) {
+    if (o.operand_bits >= 0) return CAPS_OK;
+    o.operand_bits = 0;
+    const int m = d.lda >> d.nrec;
+    if (o.form != CAPS_FORM_SPLIT || o.slices > 0 || o.split_scheme == CAPS_SPLIT_DIGITS ||
+        (m + 15) / 16 * 16 > RESIDUE_KMAX)
+        return CAPS_OK;
+    CAPS_TRY(status_buffer());
+    ClassCfg c{};
+    CAPS_TRY(tune_size(m, o, c, true));
+    o.operand_bits = c.bits;
     return CAPS_OK;
 }
 
@@ -1727,6 +1761,7 @@ caps_status caps_autotune_info(int index, caps_tune_info *out) {
         out->operand_bits = t.bits > 0 ? t.bits : 55;
         out->moduli = crt_moduli_needed(out->operand_bits, leaf);
         out->gate_rejected = t.rejected;
+        out->leaf_gate = t.scheme >= kLeafGateKey;
     } else {
         out->tile_rows = 128;
         out->tile_cols = 64;

@@ -78,9 +78,20 @@ typedef struct caps_options {
     int plain_tile;            /* plain form: the DMMA base case's CTA tile, caps_plain_tile */
     int operand_bits;          /* split form, residue scheme: cap on the operand bits, 0 = 55
                                   (the data's own need when lower); fewer bits take fewer moduli
-                                  and round the operands more coarsely.  1..55 */
+                                  and round the operands more coarsely.  1..55, or
+                                  CAPS_OPERAND_BITS_TUNED */
     long long reserved[3];
 } caps_options;
+
+/* caps_options.operand_bits: the library picks 55, 52 or 48 bits per leaf
+ * size -- the fewest (fewest moduli: 17 / 16 / 15) that run faster than 55
+ * and whose leaf product, on synthetic uniform and wide-range (u 2^k,
+ * |k| <= 20) leaves, is no less accurate than the FP64 DMMA leaf's (squared
+ * error sum and largest entry error against a 55-bit reference).  Timed and
+ * checked on the device once per leaf size and device, and kept with the
+ * autotuner's choices (caps_autotune_info, leaf_gate = 1); make the first
+ * such call for a leaf size outside any stream capture. */
+#define CAPS_OPERAND_BITS_TUNED (-1)
 
 /* CTA tiles of the plain form's DMMA base case. */
 typedef enum caps_plain_tile {
@@ -202,8 +213,10 @@ void caps_set_phase_timing(int enable);
 
 /* Batched independent multiplies of uneven sizes.  Matrices i use A[i],
  * B[i], C[i] (device, column-major n[i] x n[i]).  Instances are grouped by
- * size; the autotuner picks recursion depth and b/d pattern per size (timed
- * on first use, cached per process); each size class runs as one batched
+ * size; the autotuner picks depth, b/d pattern, split scheme, DMMA tile and
+ * residue operand bits per size (caps_autotune_info; timed on first use,
+ * kept per process and on disk), overriding those fields of `opt`; each
+ * size class runs as one batched
  * recursion whose base case is a persistent GEMM launch; the whole batch is
  * captured once as a CUDA graph and replayed while the same sizes and
  * pointers come back.  Synchronises `stream` before returning.  No
@@ -242,6 +255,8 @@ typedef struct {
     int operand_bits;   /* residues: operand bits per entry (55, or a smaller cap that won); else 0 */
     int moduli;         /* residues: moduli per leaf product for float data at that cap; else 0 */
     int gate_rejected;  /* residues: smaller bit caps that ran faster but failed the accuracy gate */
+    int leaf_gate;      /* 1: the operand-bit choice for single multiplies' leaves of n
+                           (CAPS_OPERAND_BITS_TUNED), not a batched size class */
     int from_cache;     /* 1: read from the on-disk cache */
     double seconds;     /* per instance, of the choice */
 } caps_tune_info;

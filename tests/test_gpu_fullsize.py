@@ -10,7 +10,8 @@ properties that do not need a full classical product:
   - n = 16384, r = 3, split and plain forms, on uniform[-1,1) inputs and on
     wide-range inputs u 2^k (k uniform in [-20, 20]): the split form's error
     is no worse than the plain form's, elementwise and normwise, over 1024
-    sampled entries;
+    sampled entries, with 55-bit operands and with the library's
+    accuracy-gated operand bits;
   - n = 32768, r = 4, 'bbdd' under a 120 GB workspace budget (-m 120000),
     integers in [-1024, 1024]: 256 sampled entries of both forms equal the
     exact int64 dot products (fromfile1.cpp:124-145 checks its known answers
@@ -74,8 +75,11 @@ def test_fullsize_plain_n8192_ddd_error_with_cpu_strassen(caps, oracle_mod, cuda
     assert ew < 1e-14
 
 
+@pytest.mark.parametrize("bits", [0, -1])
 @pytest.mark.parametrize("wide", [False, True])
-def test_fullsize_split_n16384_error_no_worse_than_plain(caps, oracle_mod, cuda, wide):
+def test_fullsize_split_n16384_error_no_worse_than_plain(caps, oracle_mod, cuda, wide, bits):
+    """bits 0: 55-bit operands (17 moduli); -1: the library's accuracy-gated
+    choice for leaves of 2048, as the benchmark runs it."""
     import torch
     n, r = 16384, 3
     d = caps.MatDescriptor.make(n, r)
@@ -84,10 +88,10 @@ def test_fullsize_split_n16384_error_no_worse_than_plain(caps, oracle_mod, cuda,
     A_cm, B_cm = _colmajor_host(caps, A, d), _colmajor_host(caps, B, d)
     err = {}
     for form in ("split", "plain"):
-        caps.multiply(A, B, C, d, None, form=form)
+        caps.multiply(A, B, C, d, None, form=form, operand_bits=bits)
         torch.cuda.synchronize()
         if form == "split":
-            assert caps.counters()["split_moduli"] == 17
+            assert caps.counters()["split_moduli"] == 17 if bits == 0 else caps.counters()["split_moduli"] in (15, 16, 17)
         err[form] = _sampled_error(oracle_mod, _colmajor_host(caps, C, d), A_cm, B_cm, n, 1024, 9)
     del A, B, C
     caps.release_cache()

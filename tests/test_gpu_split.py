@@ -167,6 +167,26 @@ def test_residue_leaf_operand_bit_cap_bitexact_vs_model(caps, oracle_mod, cuda, 
     assert np.array_equal(C, (Ai.astype(np.int64) @ Bi.astype(np.int64)).astype(np.float64))
 
 
+def test_residue_leaf_tuned_operand_bits(caps, oracle_mod, cuda):
+    """operand_bits = -1: the library gates 55 / 52 / 48 bits once for leaves
+    of 1024, records the choice (leaf_gate), and the product equals the
+    oracle's 128-bit model at the chosen cap; a second call reuses it."""
+    m = 1024
+    rng = np.random.default_rng(17)
+    A = rng.uniform(-1, 1, (m, m))
+    B = rng.uniform(-1, 1, (m, m))
+    C, cnt = _leaf(caps, cuda, A, B, operand_bits=-1)
+    tab = [t for t in caps.autotune_table() if t["leaf_gate"] and t["n"] == m]
+    assert len(tab) == 1 and tab[0]["scheme"] == "residues" and tab[0]["operand_bits"] in (55, 52, 48)
+    bits = tab[0]["operand_bits"]
+    assert cnt["split_moduli"] == expected_moduli(bits, bits, m)
+    ref, _ = _residue_ref(oracle_mod, A, B, bits)
+    assert np.array_equal(C, ref)
+    C2, _ = _leaf(caps, cuda, A, B, operand_bits=-1)
+    assert np.array_equal(C2, C)
+    assert len([t for t in caps.autotune_table() if t["leaf_gate"] and t["n"] == m]) == 1
+
+
 @pytest.mark.parametrize("m", [128, 64, 14, 200, 512, 1100, 2048])
 def test_residue_leaf_bitexact_vs_model_uniform(caps, oracle_mod, cuda, m):
     rng = np.random.default_rng(100 + m)

@@ -212,9 +212,10 @@ def test_tile_and_operand_bits_validated(caps):
     out = ctypes.c_longlong()
     for kw, status in (({"tile": 2}, 0), ({"tile": "32x32"}, 0), ({"tile": 3}, 8), ({"tile": -1}, 8),
                        ({"operand_bits": 48}, 0), ({"operand_bits": 55}, 0), ({"operand_bits": 56}, 8),
-                       ({"operand_bits": -1}, 8)):
+                       ({"operand_bits": -1}, 0), ({"operand_bits": -2}, 8)):
         opt = caps.options("split", **kw)
         assert L.caps_workspace_size(d, b"b", ctypes.byref(opt), ctypes.byref(out)) == status, kw
-    # the tuner's table is empty before any batched call
+    # -1 (CAPS_OPERAND_BITS_TUNED) is the library's choice: accepted; sizing a
+    # workspace tunes nothing, so the tuner's table stays empty
     assert caps.autotune_table() == []
     assert L.caps_autotune_info(0, None) == 8
