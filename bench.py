@@ -498,7 +498,8 @@ def run_chol16384(args, world, rank, local):
     hC.copy_(C0)
 
     def step():
-        cg.chol_mult(C, A, B, n, r, 1.0, form="split", stream=stream.cuda_stream, scheme=args.scheme)
+        cg.chol_mult(C, A, B, n, r, 1.0, form="split", stream=stream.cuda_stream, scheme=args.scheme,
+                     operand_bits=args.operand_bits)
 
     for _ in range(max(args.warmup, 3)):
         step()
@@ -522,14 +523,16 @@ def run_chol16384(args, world, rank, local):
     t = max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps, world)
     moduli = cg.counters()["split_moduli"]
     pattern = cg.resolve_pattern(desc, None, form="split")
+    gate = [e for e in cg.autotune_table() if e["leaf_gate"] and e["n"] == n >> r]
+    bits_used = (gate[-1]["operand_bits"] if gate else 55) if args.operand_bits < 0 else (args.operand_bits or 55)
 
     # e2e: the host entry point with pinned host buffers (A, B, C in; C out)
     nA, nB, nC = hA.numpy(), hB.numpy(), hC.numpy()
-    cg.chol_mult(nC, nA, nB, n, r, 1.0, form="split", scheme=args.scheme)
+    cg.chol_mult(nC, nA, nB, n, r, 1.0, form="split", scheme=args.scheme, operand_bits=args.operand_bits)
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        cg.chol_mult(nC, nA, nB, n, r, 1.0, form="split", scheme=args.scheme)
+        cg.chol_mult(nC, nA, nB, n, r, 1.0, form="split", scheme=args.scheme, operand_bits=args.operand_bits)
     t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
     if rank != 0:
         return
@@ -578,6 +581,8 @@ def run_chol16384(args, world, rank, local):
         {"workload": "cholesky mult() C = C - A B^T, n=16384, r=3 recursive layout, split form "
                      "(residues modulo %d moduli)" % moduli, "n": n, "nrec": r, "pattern": pattern,
          "form": "split", "alpha": 1.0, "inputs": "float64 uniform[-1,1) seeded (torch.Generator)",
+         "operand_bits": bits_used, "operand_bits_choice": "library's accuracy-gated choice per leaf size"
+         if args.operand_bits < 0 else "fixed by --operand-bits",
          "l2": "inputs larger than L2 (each matrix 2 GiB vs 129 MB L2)"},
         error=err,
         roofline={"bound": "tensor", "kernel": "crt_gemm_kernel" if moduli else "split_gemm_kernel",

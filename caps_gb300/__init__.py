@@ -250,14 +250,14 @@ def leaf_gemm(A, B, C, m: int, form: int | str = CAPS_FORM_PLAIN, slices: int = 
 
 def chol_mult(C, A, B, n: int, r: int, alpha: float = 1.0, x: int = 1, pattern=None,
               form: int | str = CAPS_FORM_PLAIN, slices: int = 0, diagonals: int = 0, stream=None,
-              scheme: int | str = 0) -> None:
+              scheme: int | str = 0, operand_bits: int = 0) -> None:
     """The Cholesky subproject's multiply (cholesky/mult.h:6, mult.cpp:11-28 on
     one rank): C = alpha C - A B^T on n x n matrices in its recursive layout
     with r levels (the CAPS layout with nrec = r, bs = 1).  The product runs
     as this library's Strassen-Winograd multiply with r levels.  alpha = 0
     leaves C unread.  Torch CUDA tensors run on `stream`; numpy arrays go
-    through the host entry point."""
-    opt = options(form, slices, diagonals, 0, scheme)
+    through the host entry point.  operand_bits: see options()."""
+    opt = options(form, slices, diagonals, 0, scheme, 0, operand_bits)
     if isinstance(A, np.ndarray):
         for t in (A, B, C):
             if t.dtype != np.float64 or not t.flags.c_contiguous:
