@@ -223,6 +223,31 @@ __global__ void crt_resolve_kernel(char *__restrict__ ws, Geo g, SplitParams p) 
 }
 
 // ---------------------------------------------------------------- slice
+// The residues of 8 values modulo each of the first NL moduli (A side:
+// premultiplied by the CRT coefficients of NL moduli), 8 bf16 per plane.
+template <int NL>
+__device__ __forceinline__ void write_residues_unrolled(const Limbs (&x)[8], char *dst, size_t plane_stride,
+                                                        int side) {
+    if (side == 0) {
+#pragma unroll
+        for (int l = 0; l < NL; l++) {
+            uint32_t w[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                w[q] = pack_bf16x2(residue_y_f32(x[2 * q], NL, l), residue_y_f32(x[2 * q + 1], NL, l));
+            *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+    } else {
+#pragma unroll
+        for (int l = 0; l < NL; l++) {
+            uint32_t w[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) w[q] = pack_bf16x2(residue_f32(x[2 * q], l), residue_f32(x[2 * q + 1], l));
+            *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+    }
+}
+
 // Residue planes, per modulus l:
 //   A: [l][mt][ks] tiles of 128 x 16 (4 KiB), B: [l][rt][ks] tiles of 256 x 16
 //   (8 KiB), each the UMMA canonical K-major image (8-row x 16-byte core
@@ -281,45 +306,33 @@ __device__ __forceinline__ void crt_slice_tile(const LeafTask *__restrict__ task
     Limbs x[8];
 #pragma unroll
     for (int e = 0; e < 8; e++) x[e] = limbs14(scaled_round(v[e], f));
-    if (L == LMAX) {
-        // float data always needs every modulus: unrolled, the FMAs take the
-        // constants straight from the constant bank
-        if (side == 0) {
-#pragma unroll
-            for (int l = 0; l < LMAX; l++) {
-                uint32_t w[4];
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    w[q] = pack_bf16x2(residue_y_f32(x[2 * q], LMAX, l), residue_y_f32(x[2 * q + 1], LMAX, l));
-                *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
-            }
-        } else {
-#pragma unroll
-            for (int l = 0; l < LMAX; l++) {
-                uint32_t w[4];
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    w[q] = pack_bf16x2(residue_f32(x[2 * q], l), residue_f32(x[2 * q + 1], l));
-                *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
-            }
-        }
-    } else if (side == 0) {
+    switch (L) {
+        // float data need 17 moduli at 55 bits, 16 or 15 under an operand-bit
+        // cap: unrolled, the FMAs take their constants straight from the
+        // constant bank, with no per-modulus loads or loop bookkeeping
+        case 17: write_residues_unrolled<17>(x, dst, plane_stride, side); break;
+        case 16: write_residues_unrolled<16>(x, dst, plane_stride, side); break;
+        case 15: write_residues_unrolled<15>(x, dst, plane_stride, side); break;
+        default:
+            if (side == 0) {
 #pragma unroll 1
-        for (int l = 0; l < L; l++) {
-            uint32_t w[4];
+                for (int l = 0; l < L; l++) {
+                    uint32_t w[4];
 #pragma unroll
-            for (int q = 0; q < 4; q++)
-                w[q] = pack_bf16x2(residue_y_f32(x[2 * q], L, l), residue_y_f32(x[2 * q + 1], L, l));
-            *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
-        }
-    } else {
+                    for (int q = 0; q < 4; q++)
+                        w[q] = pack_bf16x2(residue_y_f32(x[2 * q], L, l), residue_y_f32(x[2 * q + 1], L, l));
+                    *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
+                }
+            } else {
 #pragma unroll 1
-        for (int l = 0; l < L; l++) {
-            uint32_t w[4];
+                for (int l = 0; l < L; l++) {
+                    uint32_t w[4];
 #pragma unroll
-            for (int q = 0; q < 4; q++) w[q] = pack_bf16x2(residue_f32(x[2 * q], l), residue_f32(x[2 * q + 1], l));
-            *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
-        }
+                    for (int q = 0; q < 4; q++)
+                        w[q] = pack_bf16x2(residue_f32(x[2 * q], l), residue_f32(x[2 * q + 1], l));
+                    *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
+                }
+            }
     }
 }
 
