@@ -24,6 +24,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -120,10 +121,18 @@ enum OpKind { K_EW = 0, K_LEAF_DMMA, K_LEAF_SPLIT, K_REORDER, K_WAIT, K_RECORD }
 // Events the host entry point uses to overlap its copies with a top-level
 // 'd' step: the step waits for A11/B11 (0) before Q1, for A12/B21 (1) before
 // Q2 and for the other input quadrants (2) before forming T4/S4; it records
-// when C11 (3), C22 (4), C21 (5) and C12 (6) are final so their copies back
-// run under the later subproducts.
-constexpr int HOST_EVENTS = 7;
-constexpr int EV_C_FIRST = 3;  // events 3..6: C11, C22, C21, C12 final
+// when C11 (3), C22 (4) and C21 (5) are final, so their copies back run under
+// the later subproducts, and C12, the last, in four parts (6..9): its final
+// sum runs as four launches, and each part's copy back runs under the next.
+constexpr int C12_PARTS = 4;
+constexpr int HOST_EVENTS = 6 + C12_PARTS;
+constexpr int EV_C_FIRST = 3;  // events 3..5: C11, C22, C21 final; 6..9: the parts of C12
+
+// Part k of C12's q elements: [c12_part_begin(q, k), c12_part_begin(q, k + 1)),
+// boundaries on even elements so that the parts keep 16-byte alignment.
+static int64_t c12_part_begin(int64_t q, int k) {
+    return k >= C12_PARTS ? q : (q * k / C12_PARTS) & ~(int64_t)1;
+}
 enum Phase { PH_ADD = 0, PH_MUL = 1, PH_REARRANGE = 2 };
 
 struct Op {
@@ -460,8 +469,17 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
         if (top) emit_event(b, K_RECORD, EV_C_FIRST + 2);  // C21 final
         form(EW_FORM_T6);
         sub(6);
-        comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C12; t.src[1] = d.Q; t.dst[0] = d.C12; });
-        if (top) emit_event(b, K_RECORD, EV_C_FIRST + 3);  // C12 final
+        if (top) {
+            // C12 = U3 + Q6 in parts, each recorded when final
+            for (int k = 0; k < C12_PARTS; k++) {
+                const int64_t p0 = c12_part_begin(q, k), p1 = c12_part_begin(q, k + 1);
+                if (p1 > p0)
+                    emit_ew(b, EW_ADD, {EwTask{{nd[0].C12 + p0, nd[0].Q + p0}, {nd[0].C12 + p0}}}, p1 - p0);
+                emit_event(b, K_RECORD, EV_C_FIRST + 3 + k);
+            }
+        } else {
+            comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C12; t.src[1] = d.Q; t.dst[0] = d.C12; });
+        }
         if (!top) {
             sub(2);
             comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = d.Q; t.dst[0] = d.C11; });
@@ -729,9 +747,16 @@ static caps_status launch_ops(const std::vector<Op> &ops, char *tables, char *ws
     return CAPS_OK;
 }
 
-static caps_status run_ops(Planned &pl, cudaStream_t s, double *phase_time, KernelTiming *kt) {
+// Work a caller enqueues once the plan's tables are on their way and before
+// its kernels (the host entry point's input copies: queued after the tables,
+// they cannot hold the tables' copy up behind gigabytes of inputs).
+using AfterUpload = std::function<caps_status()>;
+
+static caps_status run_ops(Planned &pl, cudaStream_t s, double *phase_time, KernelTiming *kt,
+                           const AfterUpload &after_upload = nullptr) {
     char *tables = g_arena.ptr + pl.table_off;
     CAPS_TRY(upload_tables(pl.b.blob, tables, s));
+    if (after_upload) CAPS_TRY(after_upload());
     return launch_ops(pl.b.ops, tables, g_arena.ptr, s, phase_time, kt);
 }
 
@@ -771,7 +796,8 @@ static caps_status resolve_operand_bits(const caps_desc &d, caps_options &o);
 
 static caps_status multiply_dev_locked(const double *A, const double *B, double *C, caps_desc d,
                                        const char *pattern, const caps_options &o_in, cudaStream_t s,
-                                       bool sync_status, bool host_overlap = false) {
+                                       bool sync_status, bool host_overlap = false,
+                                       const AfterUpload &after_upload = nullptr) {
     CAPS_TRY(check_desc(d));
     CAPS_TRY(check_pattern(d, pattern));
     CAPS_TRY(check_opts(o_in));
@@ -797,7 +823,7 @@ static caps_status multiply_dev_locked(const double *A, const double *B, double 
     double pt[3] = {0, 0, 0};
     long long l0 = g_launches;
     KernelTiming kt;
-    CAPS_TRY(run_ops(pl, s, g_phase_timing ? pt : nullptr, g_phase_timing ? &kt : nullptr));
+    CAPS_TRY(run_ops(pl, s, g_phase_timing ? pt : nullptr, g_phase_timing ? &kt : nullptr, after_upload));
     g_counters.time_leaf_gemm = kt.gemm_seconds;
     g_counters.leaf_gemm_launches = kt.gemm_launches;
     g_counters.leaf_gemm_m3 = kt.gemm_leaf_m3;
@@ -1501,40 +1527,53 @@ caps_status caps_multiply_host(const double *A, const double *B, double *C, caps
     const bool timeline = g_phase_timing;  // where the call's time goes (timing events)
     g_counters.host_first_inputs = g_counters.host_all_inputs = 0;
     g_counters.host_compute_end = g_counters.host_copy_back_end = 0;
-    CAPS_CUDA_TRY(cudaEventRecord(start, s));  // after earlier work on s
-    CAPS_CUDA_TRY(cudaStreamWaitEvent(cs, start, 0));
-    if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[0], cs));
-    // quadrants X11, X21, X12, X22 at 0, q, 2q, 3q: A11 + B11 (Q1), then
-    // A12 + B21 (Q2), then the rest
-    CAPS_CUDA_TRY(h2d(dA, A, 0));
-    CAPS_CUDA_TRY(h2d(dB, B, 0));
-    CAPS_CUDA_TRY(cudaEventRecord(g_host_events[0], cs));
-    if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[1], cs));
-    CAPS_CUDA_TRY(h2d(dA, A, 2));
-    CAPS_CUDA_TRY(h2d(dB, B, 1));
-    CAPS_CUDA_TRY(cudaEventRecord(g_host_events[1], cs));
-    CAPS_CUDA_TRY(h2d(dA, A, 1));
-    CAPS_CUDA_TRY(h2d(dA, A, 3));
-    CAPS_CUDA_TRY(h2d(dB, B, 2));
-    CAPS_CUDA_TRY(h2d(dB, B, 3));
-    CAPS_CUDA_TRY(cudaEventRecord(g_host_events[2], cs));
-    if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[2], cs));
+    if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[0], s));  // the call's start
+    // The input copies, enqueued once the plan's tables are queued on s (a
+    // copy queued later on s waits behind these in the host-to-device copy
+    // engine).  Quadrants X11, X21, X12, X22 at 0, q, 2q, 3q: A11 + B11 (Q1),
+    // then A12 + B21 (Q2), then the rest.
+    const AfterUpload inputs = [&]() -> caps_status {
+        CAPS_CUDA_TRY(cudaEventRecord(start, s));  // after earlier work on s
+        CAPS_CUDA_TRY(cudaStreamWaitEvent(cs, start, 0));
+        CAPS_CUDA_TRY(h2d(dA, A, 0));
+        CAPS_CUDA_TRY(h2d(dB, B, 0));
+        CAPS_CUDA_TRY(cudaEventRecord(g_host_events[0], cs));
+        if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[1], cs));
+        CAPS_CUDA_TRY(h2d(dA, A, 2));
+        CAPS_CUDA_TRY(h2d(dB, B, 1));
+        CAPS_CUDA_TRY(cudaEventRecord(g_host_events[1], cs));
+        CAPS_CUDA_TRY(h2d(dA, A, 1));
+        CAPS_CUDA_TRY(h2d(dA, A, 3));
+        CAPS_CUDA_TRY(h2d(dB, B, 2));
+        CAPS_CUDA_TRY(h2d(dB, B, 3));
+        CAPS_CUDA_TRY(cudaEventRecord(g_host_events[2], cs));
+        if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[2], cs));
+        return CAPS_OK;
+    };
     // the plan's own phase timing would synchronise inside the call and
     // serialise the copies back behind the whole multiply: off here
     g_phase_timing = false;
-    caps_status st = multiply_dev_locked(dA, dB, dC, desc, pat, o, s, false, true);
+    caps_status st = multiply_dev_locked(dA, dB, dC, desc, pat, o, s, false, true, inputs);
     g_phase_timing = timeline;
     if (st != CAPS_OK) {
         cudaStreamSynchronize(cs);
         return st;
     }
     if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[3], s));
-    // C11 (quadrant 0), C22 (3), C21 (1), C12 (2) as they become final
-    const int quad_of_event[HOST_EVENTS - EV_C_FIRST] = {0, 3, 1, 2};
-    for (int e = EV_C_FIRST; e < HOST_EVENTS; e++) {
+    // C11 (quadrant 0), C22 (3), C21 (1) as they become final, then C12 (2)
+    // part by part
+    const int quad_of_event[3] = {0, 3, 1};
+    for (int e = EV_C_FIRST; e < EV_C_FIRST + 3; e++) {
         CAPS_CUDA_TRY(cudaStreamWaitEvent(cs, g_host_events[e], 0));
         const int quad = quad_of_event[e - EV_C_FIRST];
         CAPS_CUDA_TRY(cudaMemcpyAsync((char *)C + quad * q, (char *)dC + quad * q, q, cudaMemcpyDeviceToHost, cs));
+    }
+    const int64_t qe = (int64_t)(q / sizeof(double));  // elements per quadrant
+    for (int k = 0; k < C12_PARTS; k++) {
+        CAPS_CUDA_TRY(cudaStreamWaitEvent(cs, g_host_events[EV_C_FIRST + 3 + k], 0));
+        const size_t b0 = (size_t)c12_part_begin(qe, k) * sizeof(double), b1 = (size_t)c12_part_begin(qe, k + 1) * sizeof(double);
+        if (b1 > b0)
+            CAPS_CUDA_TRY(cudaMemcpyAsync((char *)C + 2 * q + b0, (char *)dC + 2 * q + b0, b1 - b0, cudaMemcpyDeviceToHost, cs));
     }
     if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[4], cs));
     if (o.form == CAPS_FORM_SPLIT) CAPS_TRY(check_device_status(s, nullptr));
@@ -1580,7 +1619,7 @@ caps_status caps_leaf_gemm_dev(const double *A, const double *B, double *C, int 
 // mult.cpp:91-98).
 static caps_status chol_mult_locked(double *C, const double *A, const double *B, int n, int x, int r,
                                     double alpha, const char *pattern, const caps_options &o, cudaStream_t s,
-                                    cudaEvent_t c_ready = nullptr) {
+                                    cudaEvent_t c_ready = nullptr, const AfterUpload &after_upload = nullptr) {
     if (!A || !B || !C) return CAPS_ERR_ARG;
     if (x != 1) {
         g_last_err = "mult: x > 1 process groups need more than one rank";
@@ -1596,7 +1635,7 @@ static caps_status chol_mult_locked(double *C, const double *A, const double *B,
     double *nbt = (double *)g_chol.ptr;
     double *prod = direct ? C : (double *)(g_chol.ptr + slot);
     CAPS_CUDA_TRY(launch_rec_transpose(B, nbt, n, r, true, s));
-    CAPS_TRY(multiply_dev_locked(A, nbt, prod, d, pattern, o, s, true));
+    CAPS_TRY(multiply_dev_locked(A, nbt, prod, d, pattern, o, s, true, false, after_upload));
     if (!direct) {
         if (c_ready) CAPS_CUDA_TRY(cudaStreamWaitEvent(s, c_ready, 0));  // C's copy, made beside the multiply
         CAPS_CUDA_TRY(launch_scale_add(C, prod, alpha, (int64_t)n * n, s));
@@ -1628,16 +1667,20 @@ caps_status caps_chol_mult_host(double *C, const double *A, const double *B, int
     const bool copy_c = alpha != 0.0;
     CAPS_CUDA_TRY(cudaMemcpyAsync(dB, B, nn, cudaMemcpyHostToDevice, s));
     CAPS_CUDA_TRY(cudaMemcpyAsync(dA, A, nn, cudaMemcpyHostToDevice, s));
-    if (copy_c) {
-        // after A and B are in (the copies share the host link) and after earlier
-        // work on s, so dC is free
+    // C's copy, enqueued once the product's task tables are queued on s: a
+    // copy queued on s after it would wait behind its gigabytes in the
+    // host-to-device copy engine and hold the product back
+    const AfterUpload c_copy = [&]() -> caps_status {
+        // after A and B are in (the copies share the host link) and after
+        // earlier work on s, so dC is free
         CAPS_CUDA_TRY(cudaEventRecord(start, s));
         CAPS_CUDA_TRY(cudaStreamWaitEvent(cs, start, 0));
         CAPS_CUDA_TRY(cudaMemcpyAsync(dC, C, nn, cudaMemcpyHostToDevice, cs));
         CAPS_CUDA_TRY(cudaEventRecord(c_ready, cs));
-    }
+        return CAPS_OK;
+    };
     caps_status st = chol_mult_locked(dC, dA, dB, n, x, r, alpha, pattern, opts_or_default(opt), s,
-                                      copy_c ? c_ready : nullptr);
+                                      copy_c ? c_ready : nullptr, copy_c ? c_copy : AfterUpload());
     if (st != CAPS_OK) {
         cudaStreamSynchronize(cs);
         return st;

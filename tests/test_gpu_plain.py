@@ -174,12 +174,14 @@ def test_host_entry_point_matches_device(caps, oracle_mod, cuda):
     assert np.array_equal(mat_of(oracle_mod, c, n, r), (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64))
 
 
+@pytest.mark.parametrize("n,r", [(512, 3), (198, 1)])
 @pytest.mark.parametrize("form", ["plain", "split"])
-def test_host_entry_default_pattern_overlapped_copies(caps, oracle_mod, cuda, form):
+def test_host_entry_default_pattern_overlapped_copies(caps, oracle_mod, cuda, form, n, r):
     """No pattern: the library's choice, a top-level 'd' step with the copies
-    overlapping the subproducts.  Integer inputs, exact; and a second call
-    with other inputs (the copy stream and events are reused)."""
-    n, r = 512, 3
+    overlapping the subproducts (C12 comes back in four parts).  Integer
+    inputs, exact; and a second call with other inputs (the copy stream and
+    events are reused).  n = 198: quadrants of 99^2, an odd element count,
+    so the parts of C12 have uneven lengths."""
     for seed in (11, 12):
         rng = np.random.default_rng(seed)
         A = rng.integers(-100, 101, (n, n)).astype(np.float64)
