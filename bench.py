@@ -743,8 +743,9 @@ def main():
     e2e_timeline = {"wall_ms": tl_wall, "first_inputs_ms": tc["host_first_inputs"] * 1e3,
                     "all_inputs_ms": tc["host_all_inputs"] * 1e3, "compute_end_ms": tc["host_compute_end"] * 1e3,
                     "copy_back_end_ms": tc["host_copy_back_end"] * 1e3,
-                    "meaning": "device times from the call's start: A11+B11 on the device, all inputs on the "
-                               "device, last kernel done, last C quadrant on the host"}
+                    "meaning": "device times from the call's start: the first inputs Q1 waits for on the device "
+                               "(the first sub-quadrants of A11 and B11), all inputs on the device, last kernel "
+                               "done, last C quadrant on the host"}
     barrier(world)
 
     # ---- plain FP64 Strassen of the same multiply, and the errors of both
@@ -854,7 +855,8 @@ def main():
                     "pinned_copy_gbs_after_e2e": copy_bw_after,
                     "pinned_copy_gbs_after_error_checks": out.get("copy_bw_late"),
                     "api": "caps_multiply_host, pinned host buffers, no pattern given: top level 'd' + %s "
-                           "with copies overlapped" % e2e_pattern[1:]},
+                           "with copies overlapped (its first subproduct a 'd' step too, started on the first "
+                           "sub-quadrants of A11 and B11)" % e2e_pattern[1:]},
             "gpu_launches": launches,
             "clocks": clk.summary(),
         }

@@ -125,8 +125,13 @@ enum OpKind { K_EW = 0, K_LEAF_DMMA, K_LEAF_SPLIT, K_REORDER, K_WAIT, K_RECORD }
 // the later subproducts, and C12, the last, in four parts (6..9): its final
 // sum runs as four launches, and each part's copy back runs under the next.
 constexpr int C12_PARTS = 4;
-constexpr int HOST_EVENTS = 6 + C12_PARTS;
 constexpr int EV_C_FIRST = 3;  // events 3..5: C11, C22, C21 final; 6..9: the parts of C12
+// With a level below the top step, its first subproduct Q1 = A11 B11 runs as
+// an overlapped lean step too, on the sub-quadrants of A11 and B11: events
+// EV_INNER (A11's and B11's first sub-quadrants), +1 (A11's 12 and B11's 21),
+// +2 (the rest of A11 and B11).
+constexpr int EV_INNER = 6 + C12_PARTS;
+constexpr int HOST_EVENTS = EV_INNER + 3;
 
 // Part k of C12's q elements: [c12_part_begin(q, k), c12_part_begin(q, k + 1)),
 // boundaries on even elements so that the parts keep 16-byte alignment.
@@ -168,6 +173,7 @@ struct Builder {
     long long adds = 0, muls = 0, add_bytes = 0;
     int split_group = 0;
     bool host_overlap = false;  // emit K_WAIT / K_RECORD at the top-level 'd' step
+    int overlap_stage = 0;      // 0: top step not built yet; 1: building its Q1; 2: no more waits
     int hybrid = 1;             // subproducts an 'h' step runs at once (desc.nproc_summa)
 
     size_t mark() const { return top; }
@@ -439,22 +445,44 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
         // Q1 = A11 B11 and Q2 = A12 B21 run first (Q2 into a buffer of its
         // own) while the rest is copied, and C11 = Q1 + Q2 is final as soon as
         // U1 = C11 + Q4 has read Q1 -- the same sums as below, where Q2 comes
-        // last to save the buffer.
-        const bool top = b.host_overlap && P.size() == 1 && b.ops.empty();
-        double *Q2top = top ? b.alloc(q) : nullptr;
-        if (top) emit_event(b, K_WAIT, 0);  // A11, B11 on the device
-        sub(1);
-        if (top) {
-            emit_event(b, K_WAIT, 1);  // A12, B21
+        // last to save the buffer.  Stage 0 is that top step: it waits for the
+        // input events 0, 1, 2 and records when each C quadrant is final.
+        // With a level below, Q1 runs the same way one level down (stage 1,
+        // input events EV_INNER..+2 on the sub-quadrants of A11 and B11), so
+        // the first products start after a quarter of A11 and B11 is in.
+        int stage = -1;
+        if (b.host_overlap && P.size() == 1) {
+            if (b.overlap_stage == 0 && b.ops.empty()) stage = 0;
+            else if (b.overlap_stage == 1) stage = 1;
+        }
+        const bool top = stage == 0, lead = stage >= 0;
+        const int ev = stage == 1 ? EV_INNER : 0;
+        double *Q2top = lead ? b.alloc(q) : nullptr;
+        if (top && nrec >= 2) {
+            // Q1 as a lean step with the sub-quadrant waits (a 'b' and a 'd'
+            // step give the same result for the same subproducts)
+            char p1[32];
+            snprintf(p1, sizeof p1, "%s", pat + 1);
+            p1[0] = 'd';
+            b.overlap_stage = 1;
+            build(b, {{nd[0].A11, nd[0].B11, nd[0].C11}}, h, nrec - 1, p1);
+            b.overlap_stage = 2;
+        } else {
+            if (lead) emit_event(b, K_WAIT, ev);  // A11, B11 on the device
+            b.overlap_stage = 2;                  // below this step: no waits
+            sub(1);
+        }
+        if (lead) {
+            emit_event(b, K_WAIT, ev + 1);  // A12, B21
             build(b, {{nd[0].A12, nd[0].B21, Q2top}}, h, nrec - 1, pat + 1);
-            emit_event(b, K_WAIT, 2);  // A21, A22, B11, B12, B22
+            emit_event(b, K_WAIT, ev + 2);  // A21, A22, B11, B12, B22
         }
         form(EW_FORM_T4S4);
         sub(4);
         comb(EW_ADD_DUP, [](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = d.Q; t.dst[0] = d.C22; t.dst[1] = d.C12; });
-        if (top) {
+        if (lead) {
             comb(EW_ADD, [&](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = Q2top; t.dst[0] = d.C11; });
-            emit_event(b, K_RECORD, EV_C_FIRST);  // C11 final
+            if (top) emit_event(b, K_RECORD, EV_C_FIRST);  // C11 final
         }
         form(EW_FORM_T5S5);
         sub(5);
@@ -480,7 +508,7 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
         } else {
             comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C12; t.src[1] = d.Q; t.dst[0] = d.C12; });
         }
-        if (!top) {
+        if (!lead) {
             sub(2);
             comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = d.Q; t.dst[0] = d.C11; });
         }
@@ -1532,13 +1560,35 @@ caps_status caps_multiply_host(const double *A, const double *B, double *C, caps
     // copy queued later on s waits behind these in the host-to-device copy
     // engine).  Quadrants X11, X21, X12, X22 at 0, q, 2q, 3q: A11 + B11 (Q1),
     // then A12 + B21 (Q2), then the rest.
+    // With two or more levels the plan's Q1 waits on the sub-quadrants of A11
+    // and B11 (events EV_INNER..+2): 11 and 11, then 12 and 21, then the rest.
+    const bool inner = desc.nrec >= 2;
+    const size_t q4 = q / 4;
+    auto h2d_sub = [&](double *dst, const double *src, int sub) {
+        return cudaMemcpyAsync((char *)dst + sub * q4, (const char *)src + sub * q4, q4, cudaMemcpyHostToDevice, cs);
+    };
     const AfterUpload inputs = [&]() -> caps_status {
         CAPS_CUDA_TRY(cudaEventRecord(start, s));  // after earlier work on s
         CAPS_CUDA_TRY(cudaStreamWaitEvent(cs, start, 0));
-        CAPS_CUDA_TRY(h2d(dA, A, 0));
-        CAPS_CUDA_TRY(h2d(dB, B, 0));
+        if (inner) {
+            CAPS_CUDA_TRY(h2d_sub(dA, A, 0));
+            CAPS_CUDA_TRY(h2d_sub(dB, B, 0));
+            CAPS_CUDA_TRY(cudaEventRecord(g_host_events[EV_INNER], cs));
+            if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[1], cs));
+            CAPS_CUDA_TRY(h2d_sub(dA, A, 2));
+            CAPS_CUDA_TRY(h2d_sub(dB, B, 1));
+            CAPS_CUDA_TRY(cudaEventRecord(g_host_events[EV_INNER + 1], cs));
+            CAPS_CUDA_TRY(h2d_sub(dA, A, 1));
+            CAPS_CUDA_TRY(h2d_sub(dA, A, 3));
+            CAPS_CUDA_TRY(h2d_sub(dB, B, 2));
+            CAPS_CUDA_TRY(h2d_sub(dB, B, 3));
+            CAPS_CUDA_TRY(cudaEventRecord(g_host_events[EV_INNER + 2], cs));
+        } else {
+            CAPS_CUDA_TRY(h2d(dA, A, 0));
+            CAPS_CUDA_TRY(h2d(dB, B, 0));
+            if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[1], cs));
+        }
         CAPS_CUDA_TRY(cudaEventRecord(g_host_events[0], cs));
-        if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[1], cs));
         CAPS_CUDA_TRY(h2d(dA, A, 2));
         CAPS_CUDA_TRY(h2d(dB, B, 1));
         CAPS_CUDA_TRY(cudaEventRecord(g_host_events[1], cs));

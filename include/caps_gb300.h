@@ -198,8 +198,9 @@ typedef struct caps_counters {
     int split_moduli;        /* moduli used by the last split multiply's residue scheme (0: digits ran) */
     int split_pad;
     /* caps_multiply_host with phase timing on: seconds from the call's start
-     * on the device to the first input quadrants (A11, B11) being on the
-     * device, to all inputs being on the device, to the last kernel, and to
+     * on the device to the first inputs the plan waits for being on the
+     * device (A11 and B11, or their first sub-quadrants with two or more
+     * levels), to all inputs being on the device, to the last kernel, and to
      * the last C quadrant being back on the host (0 otherwise) */
     double host_first_inputs;
     double host_all_inputs;
