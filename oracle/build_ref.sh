@@ -5,6 +5,7 @@
 #   oracle/_ref/fromfile1, oracle/_ref/randombenchmark   the reference drivers
 #   oracle/_ref/libcapsref.so                           multiply() & friends
 #   oracle/_ref/libcholref.so                           cholesky/ mult() & friends
+#   oracle/_ref/librectref.so                           rect-class/ rectMM() & friends
 # Usage: oracle/build_ref.sh [REFERENCE_DIR] [THREADS]
 # REFERENCE_DIR defaults to $CAPS_REFERENCE_DIR, then to where this build's
 # container mounts the reference; the directory used is recorded in
@@ -38,6 +39,15 @@ for s in mult.cpp sizes.cpp communication.cpp counters.cpp library.cpp; do
   cobjs="$cobjs $out/chol_${s%.cpp}.o"
 done
 $CXX -shared -o "$out/libcholref.so" $cobjs $link
+# the rectangular subproject's rectMM() (rect-class/rectmm.cpp), one rank
+rect="$ref/rect-class"
+robjs=""
+for s in rectmm.cpp rectsizes.cpp; do
+  $CXX -fPIC -I"$rect" -c "$rect/$s" -o "$out/rect_${s%.cpp}.o"
+  robjs="$robjs $out/rect_${s%.cpp}.o"
+done
+$CXX -fPIC -c "$here/ref_shim/rect_comm.cpp" -o "$out/rect_comm.o"
+$CXX -shared -o "$out/librectref.so" $robjs "$out/rect_comm.o" $link
 rm -f "$out"/*.o
 echo "$ref" > "$out/REFERENCE_DIR"
 echo "built $out (threads=$threads, blas=$blaslib)"

@@ -657,3 +657,74 @@ void caps_oracle_split_gemm_residues(int64_t m, const double *A, const double *B
 {
     caps_oracle_split_gemm_residues_bits(m, A, B, C, t_out, 55);
 }
+
+/* ---------------------------------------------------------------------- */
+/* The rectangular subproject's rectMM on one rank (rect-class/rectmm.cpp). */
+/* Not Strassen: a classical recursive blocking.  Layout (rectmm.cpp:6-19   */
+/* with P = 1): at each level the m x k matrix A is a column-major grid of  */
+/* divm x divk blocks (block (M, K) at (M + K divm) x its size), B a grid  */
+/* of divk x divn, C of divm x divn; the base blocks are column-major.      */
+/* dispatch recRectMM :29-45 (r = 0: the base case; 'b'/'B' a BFS step,     */
+/* which one rank cannot take: the caller rejects it; 'd'/'D' a DFS step);  */
+/* base case localRectMM :47-51, dgemm with beta = 0; DFS step rectDFS      */
+/* :53-72, restated with its pointer walk: A advances one block per (M, K), */
+/* B one block per (K, N), C restarts at each K and advances one block per  */
+/* M, and one block (not divm blocks) per N.  So on one rank each K block   */
+/* overwrites the C block of the one before, and with divm > 1 and divn > 1 */
+/* the C blocks of neighbouring columns overlap: the last write wins.       */
+/* ---------------------------------------------------------------------- */
+static void rect_base(int64_t m, int64_t n, int64_t k, const double *A, const double *B, double *C)
+{
+    if (g_dgemm) {
+        const char N = 'N';
+        const double one = 1.0, zero = 0.0;
+        g_dgemm(&N, &N, &m, &n, &k, &one, A, &m, B, &k, &zero, C, &m);
+        return;
+    }
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+    for (int64_t j = 0; j < n; j++) {
+        double *cj = C + j * m;
+        for (int64_t i = 0; i < m; i++) cj[i] = 0.0;
+        for (int64_t kk = 0; kk < k; kk++) {
+            const double b = B[kk + j * k];
+            const double *ak = A + kk * m;
+            for (int64_t i = 0; i < m; i++) cj[i] += ak[i] * b;
+        }
+    }
+}
+
+static void rect_rec(const double *A, const double *B, double *C, int64_t m, int64_t n, int64_t k, int r,
+                     const char *patt, const int *div)
+{
+    if (r == 0) {
+        rect_base(m, n, k, A, B, C);
+        return;
+    }
+    const int divm = div[0], divn = div[1], divk = div[2];
+    const int64_t newm = m / divm, newn = n / divn, newk = k / divk;
+    const int64_t subA = newm * newk, subB = newn * newk, subC = newm * newn;
+    for (int N = 0; N < divn; N++) {
+        const double *Ap = A;
+        for (int K = 0; K < divk; K++) {
+            double *Cp = C;
+            for (int M = 0; M < divm; M++) {
+                rect_rec(Ap, B, Cp, newm, newn, newk, r - 1, patt + 1, div + 3);
+                Ap += subA;
+                Cp += subC;
+            }
+            B += subB;
+        }
+        C += subC;
+    }
+}
+
+/* C = the one-rank rectMM of A (m x k) and B (k x n), patt 'd'/'D' only,
+ * every division exact.  Returns 0, or -1 for a pattern it cannot run. */
+int caps_oracle_rect_mm(const double *A, const double *B, double *C, int64_t m, int64_t n, int64_t k, int r,
+                        const char *patt, const int *div)
+{
+    for (int l = 0; l < r; l++)
+        if (patt[l] != 'd' && patt[l] != 'D') return -1;
+    rect_rec(A, B, C, m, n, k, r, patt, div);
+    return 0;
+}

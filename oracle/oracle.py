@@ -92,6 +92,9 @@ def lib():
         L.caps_oracle_set_dgemm.restype = None
         L.caps_oracle_split_gemm_residues.restype = None
         L.caps_oracle_split_gemm_residues.argtypes = [ctypes.c_int64, _dp, _dp, _dp, ctypes.POINTER(ctypes.c_int)]
+        L.caps_oracle_rect_mm.restype = ctypes.c_int
+        L.caps_oracle_rect_mm.argtypes = [_dp, _dp, _dp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                          ctypes.c_int, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
         L.caps_oracle_split_gemm_residues_bits.restype = None
         L.caps_oracle_split_gemm_residues_bits.argtypes = [ctypes.c_int64, _dp, _dp, _dp, ctypes.POINTER(ctypes.c_int),
                                                            ctypes.c_int]
@@ -254,6 +257,21 @@ def split_gemm_residues(A_cm: np.ndarray, B_cm: np.ndarray, m: int, bits: int = 
     lib().caps_oracle_split_gemm_residues_bits(m, _p(np.ascontiguousarray(A_cm)), _p(np.ascontiguousarray(B_cm)),
                                                _p(C), t, int(bits))
     return C, (t[0], t[1])
+
+
+def rect_mm(A: np.ndarray, B: np.ndarray, C: np.ndarray, m: int, n: int, k: int, r: int, patt: str,
+            div) -> np.ndarray:
+    """One-rank rectMM (rect-class/rectmm.cpp) of A (m x k) and B (k x n) in
+    the subproject's block layout, onto a copy of C (blocks the reference
+    never writes keep C's entries).  div: 3 r division factors (m, n, k per
+    level).  Raises ValueError for a step one rank cannot take."""
+    out = np.array(C, dtype=np.float64, copy=True)
+    d = (ctypes.c_int * max(1, 3 * r))(*[int(x) for x in div])
+    st = lib().caps_oracle_rect_mm(_p(np.ascontiguousarray(A)), _p(np.ascontiguousarray(B)), _p(out), m, n, k,
+                                   int(r), patt.encode() if patt else b"", d)
+    if st:
+        raise ValueError("rectMM on one rank takes 'd' steps only")
+    return out
 
 
 # ---------------------------------------------------------------------------

@@ -17,6 +17,13 @@ one-rank build (oracle/build_ref.sh -> oracle/_ref/libcapsref.so) exist:
 4. ref_chol.npz -- outputs of the Cholesky subproject's own mult()
    (cholesky/mult.cpp, one rank; oracle/_ref/libcholref.so) on seeded
    inputs in its recursive layout: C = alpha C - A B^T.
+5. ref_rect.npz -- outputs of the rectangular subproject's own rectMM()
+   (rect-class/rectmm.cpp, one rank, DFS steps; oracle/_ref/librectref.so)
+   on seeded inputs in its block layout, C starting from seeded values.
+
+`python tests/golden/make_golden.py [REFERENCE_DIR] [NAME ...]` regenerates
+only the named fixtures (tests, float, layout, chol, rect) when names are
+given.
 """
 import ctypes
 import hashlib
@@ -146,10 +153,54 @@ def ref_chol(chollib):
     print("ref_chol.npz:", list(out))
 
 
+# The rectangular subproject's rectMM (rect-class/rectmm.cpp), one rank, DFS
+# steps: (m, n, k, r, pattern, divisions, kind, seed).  C starts from seeded
+# values: the blocks the reference's one-rank walk never writes keep them.
+RECT_CASES = [(64, 48, 32, 0, "", [], "float", 31), (64, 48, 32, 1, "d", [2, 2, 1], "float", 32),
+              (64, 48, 32, 1, "d", [1, 1, 2], "int", 33), (96, 64, 48, 2, "dd", [2, 2, 2, 3, 2, 2], "int", 34),
+              (60, 40, 24, 2, "dD", [3, 2, 1, 2, 2, 3], "float", 35),
+              (128, 128, 128, 2, "dd", [1, 2, 1, 2, 1, 1], "int", 36),
+              (256, 96, 512, 1, "d", [2, 3, 4], "float", 37)]
+
+
+def rect_inputs(m, n, k, kind, seed):
+    rng = np.random.default_rng(seed)
+    if kind == "int":
+        return [rng.integers(-9, 10, size).astype(np.float64) for size in (m * k, k * n, m * n)]
+    return [rng.uniform(-1, 1, size) for size in (m * k, k * n, m * n)]
+
+
+def ref_rect(rectlib):
+    L = ctypes.CDLL(rectlib)
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    init = getattr(L, "_Z13initSizesRectiiiiiPi")
+    init.argtypes = [ctypes.c_int] * 5 + [ip]
+    rect = getattr(L, "_Z6rectMMPdS_S_iiiiiPcPi")
+    rect.argtypes = [dp, dp, dp] + [ctypes.c_int] * 5 + [ctypes.c_char_p, ip]
+    rect.restype = None
+    out = {}
+    for m, n, k, r, patt, div, kind, seed in RECT_CASES:
+        A, B, C = rect_inputs(m, n, k, kind, seed)
+        d = (ctypes.c_int * max(1, 3 * r))(*div)
+        init(m, n, k, 1, r, d)
+        rect(A.ctypes.data_as(dp), B.ctypes.data_as(dp), C.ctypes.data_as(dp), m, n, k, 1, r, patt.encode(), d)
+        out["rect_%d_%d_%d_%d_%s_%s_%s" % (m, n, k, r, patt or "-", "".join(map(str, div)) or "-", kind)] = C
+    np.savez_compressed(os.path.join(HERE, "ref_rect.npz"), **out)
+    print("ref_rect.npz:", list(out))
+
+
 if __name__ == "__main__":
     refdir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    names = set(sys.argv[2:]) or {"tests", "float", "layout", "chol", "rect"}
     reflib = os.path.join(ROOT, "oracle", "_ref", "libcapsref.so")
-    ref_tests(refdir)
-    ref_float(reflib)
-    ref_layout(reflib)
-    ref_chol(os.path.join(ROOT, "oracle", "_ref", "libcholref.so"))
+    if "tests" in names:
+        ref_tests(refdir)
+    if "float" in names:
+        ref_float(reflib)
+    if "layout" in names:
+        ref_layout(reflib)
+    if "chol" in names:
+        ref_chol(os.path.join(ROOT, "oracle", "_ref", "libcholref.so"))
+    if "rect" in names:
+        ref_rect(os.path.join(ROOT, "oracle", "_ref", "librectref.so"))

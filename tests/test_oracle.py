@@ -284,3 +284,53 @@ def test_chol_mult_oracle_integers_exact(oracle_mod, n, r, alpha):
         finally:
             oracle_mod.use_blas(False)
         assert np.array_equal(mat_of(oracle_mod, out, n, r, 1), exact), (n, r, alpha, blas)
+
+
+def _rect_key(m, n, k, r, patt, div, kind):
+    return "rect_%d_%d_%d_%d_%s_%s_%s" % (m, n, k, r, patt or "-", "".join(map(str, div)) or "-", kind)
+
+
+def test_rect_mm_oracle_matches_reference_rectmm(oracle_mod):
+    """The restated one-rank rectMM (rect-class/rectmm.cpp) with numpy's
+    OpenBLAS reproduces the subproject's own rectMM bit for bit, including
+    its one-rank DFS walk: each k block overwriting C, and with divm, divn > 1
+    C blocks of neighbouring columns overlapping (blocks never written keep
+    C's starting values)."""
+    if not oracle_mod.use_blas(True):
+        pytest.skip("numpy OpenBLAS not found")
+    mg = _golden_module()
+    g = np.load(os.path.join(ROOT, "tests", "golden", "ref_rect.npz"))
+    try:
+        for m, n, k, r, patt, div, kind, seed in mg.RECT_CASES:
+            A, B, C = mg.rect_inputs(m, n, k, kind, seed)
+            out = oracle_mod.rect_mm(A, B, C, m, n, k, r, patt, div)
+            assert np.array_equal(out, g[_rect_key(m, n, k, r, patt, div, kind)]), (m, n, k, r, patt, div)
+    finally:
+        oracle_mod.use_blas(False)
+
+
+def test_rect_mm_oracle_quirks_and_exact_cases(oracle_mod):
+    """Integer data, classical leaves: with every divk = 1 and divm or divn
+    = 1 at every level the one-rank rectMM is the exact product in the block
+    layout; with divk = 2 only the last k block's product survives; a 'b'
+    step is rejected (one rank cannot take it)."""
+    rng = np.random.default_rng(3)
+    m, n, k = 64, 32, 48
+    A = rng.integers(-9, 10, m * k).astype(np.float64)
+    B = rng.integers(-9, 10, k * n).astype(np.float64)
+    C = np.full(m * n, np.nan)
+    # r = 1, divisions (2, 1, 1): A blocks of 32 x 48 rows stacked, B whole, C two blocks
+    out = oracle_mod.rect_mm(A, B, C, m, n, k, 1, "d", [2, 1, 1])
+    Ab = [A[i * 32 * k:(i + 1) * 32 * k].reshape(k, 32).T for i in range(2)]  # column-major blocks
+    Bm = B.reshape(n, k).T
+    for i in range(2):
+        got = out[i * 32 * n:(i + 1) * 32 * n].reshape(n, 32).T
+        assert np.array_equal(got, (Ab[i].astype(np.int64) @ Bm.astype(np.int64)).astype(np.float64))
+    # divk = 2: C = A(:, last k block) B(last k block, :), each block
+    # column-major in its own range
+    out = oracle_mod.rect_mm(A, B, C, m, n, k, 1, "d", [1, 1, 2])
+    Ak = A[m * 24:].reshape(24, m).T
+    Bk = B[24 * n:].reshape(n, 24).T
+    assert np.array_equal(out.reshape(n, m).T, (Ak.astype(np.int64) @ Bk.astype(np.int64)).astype(np.float64))
+    with pytest.raises(ValueError):
+        oracle_mod.rect_mm(A, B, C, m, n, k, 1, "b", [2, 1, 1])
