@@ -44,6 +44,7 @@ C_ABI_SYMBOLS = [
     "caps_status_string", "caps_last_cuda_error", "caps_debug_fail_allocations", "caps_release_cache",
     "caps_leaf_gemm_split_noalloc_dev", "caps_autotune_entry", "caps_chol_mult_dev", "caps_chol_mult_host",
     "caps_debug_starve_split_gemm", "caps_autotune_entry_ex", "caps_autotune_info",
+    "caps_rect_mm_dev", "caps_rect_mm_host",
 ]
 
 
@@ -154,6 +155,10 @@ def lib() -> ctypes.CDLL:
         L.caps_autotune_entry_ex.argtypes = [ctypes.c_int, ip, ip, ip, ctypes.c_char_p, ip, ip,
                                              ctypes.POINTER(ctypes.c_double)]
         L.caps_autotune_entry_ex.restype = ctypes.c_int
+        L.caps_rect_mm_dev.argtypes = [vp, vp, vp, i_, i_, i_, i_, ctypes.c_char_p, ip, vp]
+        L.caps_rect_mm_dev.restype = ctypes.c_int
+        L.caps_rect_mm_host.argtypes = [dp, dp, dp, i_, i_, i_, i_, ctypes.c_char_p, ip]
+        L.caps_rect_mm_host.restype = ctypes.c_int
         L.caps_autotune_info.argtypes = [ctypes.c_int, ctypes.POINTER(TuneInfo)]
         L.caps_autotune_info.restype = ctypes.c_int
         _lib = L
@@ -268,6 +273,27 @@ def chol_mult(C, A, B, n: int, r: int, alpha: float = 1.0, x: int = 1, pattern=N
         return
     _check(lib().caps_chol_mult_dev(_dev_ptr(C, "C"), _dev_ptr(A, "A"), _dev_ptr(B, "B"), int(n), int(x), int(r),
                                     float(alpha), _pat(pattern), ctypes.byref(opt), _stream_ptr(stream)))
+
+
+def rect_mm(A, B, C, m: int, n: int, k: int, r: int = 0, pattern: str = "", div=(), stream=None) -> None:
+    """The rectangular subproject's rectMM on one rank (rect-class/rectmm.h:1):
+    C = A B with A m x k, B k x n, C m x n in its block layout, r levels of
+    'd' steps with the division triples `div` (3 r ints: m, n, k per level).
+    Torch CUDA tensors run on `stream`; numpy arrays go through the host
+    entry point (C is copied in too: blocks the one-rank walk never writes
+    keep their entries)."""
+    d = (ctypes.c_int * max(1, 3 * int(r)))(*[int(x) for x in div])
+    pat = _pat(pattern) if r > 0 else b""
+    if isinstance(A, np.ndarray):
+        for t in (A, B, C):
+            if t.dtype != np.float64 or not t.flags.c_contiguous:
+                raise TypeError("host arrays must be contiguous float64")
+        dp = ctypes.POINTER(ctypes.c_double)
+        _check(lib().caps_rect_mm_host(A.ctypes.data_as(dp), B.ctypes.data_as(dp), C.ctypes.data_as(dp), int(m),
+                                       int(n), int(k), int(r), pat, d))
+        return
+    _check(lib().caps_rect_mm_dev(_dev_ptr(A, "A"), _dev_ptr(B, "B"), _dev_ptr(C, "C"), int(m), int(n), int(k),
+                                  int(r), pat, d, _stream_ptr(stream)))
 
 
 NOALLOC_MAX_M = 512

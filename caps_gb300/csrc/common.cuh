@@ -111,6 +111,10 @@ enum DmmaTile { DMMA_TILE_64x64 = 0, DMMA_TILE_32x32 = 1, DMMA_TILE_128x64 = 2, 
 void dmma_tile_shape(int tile, int *rows, int *cols);
 cudaError_t launch_dmma_gemm(const LeafTask *tasks_dev, int count, int m, cudaStream_t stream,
                              int tile = DMMA_TILE_64x64);
+// The same for rectangular leaves: A m x k, B k x n, C m x n (column-major,
+// leading dimensions m, k, m).
+cudaError_t launch_dmma_rect(const LeafTask *tasks_dev, int count, int m, int n, int k, cudaStream_t stream,
+                             int tile = DMMA_TILE_64x64);
 
 // Split form.  Two schemes share one launch sequence; the kernels agree on
 // the scheme through the launch group's header, written on the device after

@@ -291,3 +291,23 @@ void mult(double *C, double *A, double *B, int n, int x, int r, double alpha) {
     g_last_status = st;
     if (st != CAPS_OK) die_status(st, "mult");
 }
+
+// --------------------------------------------------------------- rect-class/rectmm.cpp
+// The rectangular subproject's rectMM on one rank (rect-class/rectmm.cpp:
+// 24-72).  An unrecognised step prints the reference's message (recRectMM
+// :41-43) and computes nothing, as the reference's walk does once every path
+// through that level stops there; other failures print and exit.
+void rectMM(double *A, double *B, double *C, int m, int n, int k, int P, int r, char *patt, int *divPatt) {
+    if (P != 1) die_status(CAPS_ERR_UNSUPPORTED, "rectMM (P > 1 needs more than one rank)");
+    caps_status st = caps_rect_mm_host(A, B, C, m, n, k, r, patt, divPatt);
+    g_last_status = st;
+    if (st == CAPS_ERR_INVALID_PATTERN) {
+        for (int l = 0; l < r; l++)
+            if (patt[l] != 'd' && patt[l] != 'D' && patt[l] != 'b' && patt[l] != 'B') {
+                printf("Error: unrecognized type of step: %c\n", patt[l]);
+                break;
+            }
+        return;
+    }
+    if (st != CAPS_OK) die_status(st, "rectMM");
+}

@@ -25,6 +25,7 @@
 #include <cstring>
 #include <deque>
 #include <functional>
+#include <unordered_map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -91,6 +92,7 @@ static DevBuf g_arena;   // workspace + task tables
 static DevBuf g_io;      // device copies for caps_multiply_host
 static DevBuf g_status;  // device status words of split kernels
 static DevBuf g_chol;    // -B^T and the product of caps_chol_mult_dev
+static DevBuf g_rect;    // task table of caps_rect_mm_dev
 
 struct PinnedBuf {
     void *ptr = nullptr;
@@ -1486,6 +1488,98 @@ static caps_status multiply_batched_locked(const std::vector<BatchItem> &items, 
     return CAPS_OK;
 }
 
+// ------------------------------------------------------------------ rectMM
+// The rectangular subproject's rectMM on one rank (rect-class/rectmm.cpp:
+// 24-72): a classical recursive blocking, not Strassen.  A (m x k), B (k x n)
+// and C (m x n) are in its block layout: at each level a column-major grid of
+// blocks (A: divm x divk, B: divk x n_blocks, C: divm x divn), the base blocks
+// column-major.  The reference's one-rank DFS walk (rectDFS :53-72) is
+// replayed on the host to list its base-case products (localRectMM :47-51,
+// beta = 0) in order.  Each overwrites its C block, so a block ends up holding
+// the last product written to it: every k block overwrites the one before,
+// and as the walk moves C one block (not divm blocks) per column block,
+// with divm, divn > 1 neighbouring columns' blocks coincide.  The last product
+// of each distinct C block runs, all in one batched DMMA launch; blocks the
+// walk never writes keep C's entries.  A BFS step needs more than one rank:
+// the reference's process split (rectBFS :75-77) leaves none.
+static caps_status rect_check(int m, int n, int k, int r, const char *patt, const int *div, int64_t leaf[3]) {
+    if (m <= 0 || n <= 0 || k <= 0 || r < 0 || r > 24) return CAPS_ERR_SIZE;
+    if (r > 0 && (!patt || !div)) return CAPS_ERR_ARG;
+    int64_t mm = m, nn = n, kk = k;
+    for (int l = 0; l < r; l++) {
+        const char c = patt[l];
+        if (c == 'b' || c == 'B') {
+            g_last_err = "rectMM: a BFS step splits the processes, and one rank has none to split";
+            return CAPS_ERR_UNSUPPORTED;
+        }
+        if (c != 'd' && c != 'D') return CAPS_ERR_INVALID_PATTERN;
+    }
+    for (int l = 0; l < r; l++) {
+        const int dm = div[3 * l], dn = div[3 * l + 1], dk = div[3 * l + 2];
+        if (dm < 1 || dn < 1 || dk < 1 || mm % dm || nn % dn || kk % dk) return CAPS_ERR_SIZE;
+        mm /= dm;
+        nn /= dn;
+        kk /= dk;
+    }
+    leaf[0] = mm;
+    leaf[1] = nn;
+    leaf[2] = kk;
+    return CAPS_OK;
+}
+
+static void rect_walk(const double *A, const double *B, double *C, int64_t m, int64_t n, int64_t k, int r,
+                      const int *div, std::vector<LeafTask> &out) {
+    if (r == 0) {
+        out.push_back({A, B, C});
+        return;
+    }
+    const int divm = div[0], divn = div[1], divk = div[2];
+    const int64_t newm = m / divm, newn = n / divn, newk = k / divk;
+    const int64_t subA = newm * newk, subB = newn * newk, subC = newm * newn;
+    for (int N = 0; N < divn; N++) {
+        const double *Ap = A;
+        for (int K = 0; K < divk; K++) {
+            double *Cp = C;
+            for (int M = 0; M < divm; M++) {
+                rect_walk(Ap, B, Cp, newm, newn, newk, r - 1, div + 3, out);
+                Ap += subA;
+                Cp += subC;
+            }
+            B += subB;
+        }
+        C += subC;
+    }
+}
+
+static caps_status rect_mm_locked(const double *A, const double *B, double *C, int m, int n, int k, int r,
+                                  const char *patt, const int *div, cudaStream_t s) {
+    int64_t leaf[3];
+    CAPS_TRY(rect_check(m, n, k, r, patt, div, leaf));
+    if (!A || !B || !C) return CAPS_ERR_ARG;
+    if (leaf[0] > INT32_MAX || leaf[1] > INT32_MAX || leaf[2] > INT32_MAX) return CAPS_ERR_SIZE;
+    std::vector<LeafTask> walk;
+    rect_walk(A, B, C, m, n, k, r, div, walk);
+    std::unordered_map<const double *, size_t> last;  // C block -> its last product
+    for (size_t i = 0; i < walk.size(); i++) last[walk[i].C] = i;
+    std::vector<uint8_t> blob;
+    for (size_t i = 0; i < walk.size(); i++) {
+        if (last[walk[i].C] != i) continue;
+        const uint8_t *p = reinterpret_cast<const uint8_t *>(&walk[i]);
+        blob.insert(blob.end(), p, p + sizeof(LeafTask));
+    }
+    const int count = (int)(blob.size() / sizeof(LeafTask));
+    CAPS_TRY(ensure(g_rect, blob.size()));
+    CAPS_TRY(upload_tables(blob, g_rect.ptr, s));
+    long long l0 = g_launches;
+    CAPS_CUDA_TRY(launch_dmma_rect(reinterpret_cast<const LeafTask *>(g_rect.ptr), count, (int)leaf[0], (int)leaf[1],
+                                   (int)leaf[2], s));
+    g_counters = caps_counters();
+    g_counters.multiplications = (long long)count * leaf[0] * leaf[1] * leaf[2];
+    g_counters.additions = g_counters.multiplications;
+    g_counters.kernel_launches = g_launches - l0;
+    return CAPS_OK;
+}
+
 }  // namespace caps
 
 using namespace caps;
@@ -1864,6 +1958,34 @@ caps_status caps_autotune_info(int index, caps_tune_info *out) {
     return CAPS_OK;
 }
 
+caps_status caps_rect_mm_dev(const double *A, const double *B, double *C, int m, int n, int k, int r,
+                             const char *pattern, const int *div_pattern, void *stream) {
+    std::lock_guard<std::recursive_mutex> g(g_mu);
+    return rect_mm_locked(A, B, C, m, n, k, r, pattern, div_pattern, (cudaStream_t)stream);
+}
+
+caps_status caps_rect_mm_host(const double *A, const double *B, double *C, int m, int n, int k, int r,
+                              const char *pattern, const int *div_pattern) {
+    std::lock_guard<std::recursive_mutex> g(g_mu);
+    int64_t leaf[3];
+    CAPS_TRY(rect_check(m, n, k, r, pattern, div_pattern, leaf));
+    if (!A || !B || !C) return CAPS_ERR_ARG;
+    const size_t ba = (size_t)m * k * sizeof(double), bb = (size_t)k * n * sizeof(double),
+                 bc = (size_t)m * n * sizeof(double);
+    const size_t oa = 0, ob = (ba + 255) & ~(size_t)255, oc = ob + ((bb + 255) & ~(size_t)255);
+    CAPS_TRY(ensure(g_io, oc + bc));
+    double *dA = (double *)(g_io.ptr + oa), *dB = (double *)(g_io.ptr + ob), *dC = (double *)(g_io.ptr + oc);
+    cudaStream_t s = 0;
+    // C too: the blocks the walk never writes keep their entries
+    CAPS_CUDA_TRY(cudaMemcpyAsync(dA, A, ba, cudaMemcpyHostToDevice, s));
+    CAPS_CUDA_TRY(cudaMemcpyAsync(dB, B, bb, cudaMemcpyHostToDevice, s));
+    CAPS_CUDA_TRY(cudaMemcpyAsync(dC, C, bc, cudaMemcpyHostToDevice, s));
+    CAPS_TRY(rect_mm_locked(dA, dB, dC, m, n, k, r, pattern, div_pattern, s));
+    CAPS_CUDA_TRY(cudaMemcpyAsync(C, dC, bc, cudaMemcpyDeviceToHost, s));
+    CAPS_CUDA_TRY(cudaStreamSynchronize(s));
+    return CAPS_OK;
+}
+
 void caps_debug_fail_allocations(int count) { g_fail_allocs = count > 0 ? count : 0; }
 
 void caps_debug_starve_split_gemm(int count) {
@@ -1876,7 +1998,7 @@ void caps_release_cache(void) {
     cudaDeviceSynchronize();
     for (BatchPlan *p : g_batch_plans) free_plan(p);
     g_batch_plans.clear();
-    for (DevBuf *b : {&g_arena, &g_io, &g_status, &g_chol}) {
+    for (DevBuf *b : {&g_arena, &g_io, &g_status, &g_chol, &g_rect}) {
         if (b->ptr) cudaFree(b->ptr);
         *b = DevBuf();
     }

@@ -1,7 +1,9 @@
 // Plain form base case: C = A * B on FP64 DMMA tensor cores (mma.sync f64).
 //
 // Replaces block_multiply -> square_dgemm_zero -> dgemm_ (multiply.cpp:
-// 1082-1141, dgemm-blas.cpp:4-13): column-major m x m operands, beta = 0.
+// 1082-1141, dgemm-blas.cpp:4-13): column-major m x m operands, beta = 0;
+// and the rectangular subproject's base case localRectMM (rect-class/
+// rectmm.cpp:47-51): A m x k, B k x n, C m x n, column-major, beta = 0.
 //
 // GB300 runs FP64 (DFMA and DMMA alike) at ~1.05 TFLOP/s for the whole GPU,
 // about 1.8 multiply-adds per clock per SM, so this kernel is bound by the
@@ -29,7 +31,8 @@ __device__ __forceinline__ void dmma_8x8x4(double (&d)[2], double a, double b) {
 }  // namespace
 
 template <int WM, int WN>
-__global__ void __launch_bounds__(32 * WM * WN) dmma_gemm_kernel(const LeafTask *__restrict__ tasks, int m) {
+__global__ void __launch_bounds__(32 * WM * WN) dmma_gemm_kernel(const LeafTask *__restrict__ tasks, int m, int n,
+                                                                 int k) {
     constexpr int BM = 32 * WM, BN = 32 * WN, NT = 32 * WM * WN;
     constexpr int LDA = BM + 8, LDB = BN + 8;  // padded rows (banks)
     __shared__ double As[BK][LDA];  // As[k][i]
@@ -38,7 +41,7 @@ __global__ void __launch_bounds__(32 * WM * WN) dmma_gemm_kernel(const LeafTask 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int wr = warp / WN, wc = warp % WN;
     const int64_t i0 = (int64_t)blockIdx.y * BM, j0 = (int64_t)blockIdx.x * BN;
-    const int64_t M = m;
+    const int64_t M = m, N = n, K = k;  // A: M x K, B: K x N, C: M x N
 
     double acc[4][4][2];
 #pragma unroll
@@ -46,21 +49,21 @@ __global__ void __launch_bounds__(32 * WM * WN) dmma_gemm_kernel(const LeafTask 
 #pragma unroll
         for (int b = 0; b < 4; b++) acc[a][b][0] = acc[a][b][1] = 0.0;
 
-    for (int64_t k0 = 0; k0 < M; k0 += BK) {
+    for (int64_t k0 = 0; k0 < K; k0 += BK) {
         // A tile: BM rows x 16 k from a column-major source; consecutive
         // threads read consecutive rows of one column
 #pragma unroll
         for (int p = 0; p < BM * BK / NT; p++) {
             const int e = tid + NT * p, row = e % BM, kk = e / BM;
             const int64_t gi = i0 + row, gk = k0 + kk;
-            As[kk][row] = (gi < M && gk < M) ? t.A[gi + gk * M] : 0.0;
+            As[kk][row] = (gi < M && gk < K) ? t.A[gi + gk * M] : 0.0;
         }
         // B tile: 16 k x BN columns; consecutive threads read the 16 k of one column
 #pragma unroll
         for (int p = 0; p < BN * BK / NT; p++) {
             const int e = tid + NT * p, kk = e % BK, col = e / BK;
             const int64_t gk = k0 + kk, gj = j0 + col;
-            Bs[kk][col] = (gk < M && gj < M) ? t.B[gk + gj * M] : 0.0;
+            Bs[kk][col] = (gk < K && gj < N) ? t.B[gk + gj * K] : 0.0;
         }
         __syncthreads();
 #pragma unroll
@@ -85,17 +88,17 @@ __global__ void __launch_bounds__(32 * WM * WN) dmma_gemm_kernel(const LeafTask 
             for (int e = 0; e < 2; e++) {
                 const int64_t gi = i0 + 32 * wr + 8 * a + (lane >> 2);
                 const int64_t gj = j0 + 32 * wc + 8 * b + 2 * (lane & 3) + e;
-                if (gi < M && gj < M) t.C[gi + gj * M] = acc[a][b][e];
+                if (gi < M && gj < N) t.C[gi + gj * M] = acc[a][b][e];
             }
 }
 
 template <int WM, int WN>
-static cudaError_t launch_dmma_shape(const LeafTask *tasks_dev, int count, int m, cudaStream_t stream) {
-    const unsigned rows = (unsigned)((m + 32 * WM - 1) / (32 * WM)), cols = (unsigned)((m + 32 * WN - 1) / (32 * WN));
+static cudaError_t launch_dmma_shape(const LeafTask *tasks_dev, int count, int m, int n, int k, cudaStream_t stream) {
+    const unsigned rows = (unsigned)((m + 32 * WM - 1) / (32 * WM)), cols = (unsigned)((n + 32 * WN - 1) / (32 * WN));
     for (int base = 0; base < count; base += 65535) {
         const int c = count - base < 65535 ? count - base : 65535;
         dim3 grid(cols, rows, (unsigned)c);
-        dmma_gemm_kernel<WM, WN><<<grid, 32 * WM * WN, 0, stream>>>(tasks_dev + base, m);
+        dmma_gemm_kernel<WM, WN><<<grid, 32 * WM * WN, 0, stream>>>(tasks_dev + base, m, n, k);
         count_launch();
     }
     return cudaGetLastError();
@@ -109,13 +112,18 @@ void dmma_tile_shape(int tile, int *rows, int *cols) {
     }
 }
 
-cudaError_t launch_dmma_gemm(const LeafTask *tasks_dev, int count, int m, cudaStream_t stream, int tile) {
-    if (count <= 0 || m <= 0) return cudaSuccess;
+cudaError_t launch_dmma_rect(const LeafTask *tasks_dev, int count, int m, int n, int k, cudaStream_t stream,
+                             int tile) {
+    if (count <= 0 || m <= 0 || n <= 0) return cudaSuccess;
     switch (tile) {
-        case DMMA_TILE_32x32: return launch_dmma_shape<1, 1>(tasks_dev, count, m, stream);
-        case DMMA_TILE_128x64: return launch_dmma_shape<4, 2>(tasks_dev, count, m, stream);
-        default: return launch_dmma_shape<2, 2>(tasks_dev, count, m, stream);
+        case DMMA_TILE_32x32: return launch_dmma_shape<1, 1>(tasks_dev, count, m, n, k, stream);
+        case DMMA_TILE_128x64: return launch_dmma_shape<4, 2>(tasks_dev, count, m, n, k, stream);
+        default: return launch_dmma_shape<2, 2>(tasks_dev, count, m, n, k, stream);
     }
+}
+
+cudaError_t launch_dmma_gemm(const LeafTask *tasks_dev, int count, int m, cudaStream_t stream, int tile) {
+    return launch_dmma_rect(tasks_dev, count, m, m, m, stream, tile);
 }
 
 }  // namespace caps

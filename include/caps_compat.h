@@ -18,6 +18,7 @@
  *                       counters.h:5-21
  *   read_timer          library.h:8          SEVEN library.h:5
  *   mult                cholesky/mult.h:6   (cholesky/mult.cpp:11-28, one rank)
+ *   rectMM              rect-class/rectmm.h:1 (rect-class/rectmm.cpp:24-72, one rank)
  *
  * Differences, all forced by one GPU per process:
  *   - one rank: getRank() = 0, getLog7nProcs() = 0, getPFactor() = 1;
@@ -50,6 +51,11 @@ void multiply(double *A, double *B, double *C, MatDescriptor desc, char *pattern
 /* The Cholesky subproject's multiply (cholesky/mult.h:6): C = alpha C - A B^T
  * on n x n host arrays in its recursive layout, one rank (x = 1). */
 void mult(double *C, double *A, double *B, int n, int x, int r, double alpha = 1.);
+
+/* The rectangular subproject's multiply (rect-class/rectmm.h:1): C = A B on
+ * host arrays in its block layout, one rank (P = 1), DFS steps; see
+ * caps_rect_mm_host. */
+void rectMM(double *A, double *B, double *C, int m, int n, int k, int P, int r, char *patt, int *divPatt);
 
 void verifyDescriptor(MatDescriptor desc);
 long long numEntriesPerProc(MatDescriptor desc);

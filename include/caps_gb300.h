@@ -226,6 +226,25 @@ caps_status caps_multiply_batched_dev(int count, const double *const *A, const d
                                       double *const *C, const int *n, const caps_options *opt,
                                       void *stream);
 
+/* The rectangular subproject's rectMM on one rank (rect-class/rectmm.h:1,
+ * rectmm.cpp:24-72): C = A B by classical recursive blocking, A m x k, B k x n,
+ * C m x n in its block layout (at each of the r levels a column-major grid of
+ * blocks, divm x divk for A, divk x divn for B, divm x divn for C, by the
+ * level's div_pattern triple; base blocks column-major), base case on FP64
+ * DMMA.  pattern: r chars, 'd'/'D' (DFS); 'b'/'B' (BFS) needs more than one
+ * rank: CAPS_ERR_UNSUPPORTED.  Every division must be exact (CAPS_ERR_SIZE).
+ * The result is the reference's on one rank, including its DFS walk: each
+ * base case writes its C block with beta = 0, so every k block overwrites
+ * the one before, and with divm, divn > 1 blocks of neighbouring columns
+ * coincide (the last product wins); blocks the walk never writes keep C's
+ * entries.  Device pointers, asynchronous on `stream`. */
+caps_status caps_rect_mm_dev(const double *A, const double *B, double *C, int m, int n, int k, int r,
+                             const char *pattern, const int *div_pattern, void *stream);
+
+/* The same on host arrays: copies A, B and C in, C back; synchronises. */
+caps_status caps_rect_mm_host(const double *A, const double *B, double *C, int m, int n, int k, int r,
+                              const char *pattern, const int *div_pattern);
+
 /* Autotuner choices made so far: entry `index` (0, 1, ...) gives the size,
  * form, recursion depth, pattern (8 bytes) and seconds per instance of the
  * winning candidate; CAPS_ERR_ARG past the last entry.  No reference

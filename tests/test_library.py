@@ -219,3 +219,50 @@ def test_tile_and_operand_bits_validated(caps):
     # workspace tunes nothing, so the tuner's table stays empty
     assert caps.autotune_table() == []
     assert L.caps_autotune_info(0, None) == 8
+
+
+def test_rect_mm_validation_before_any_device_work(caps):
+    """rectMM on one rank: a BFS step (which the reference cannot take on one
+    rank), an unknown step, and divisions that do not divide are refused
+    before anything runs."""
+    import ctypes as C
+    L = caps.lib()
+    z = C.c_void_p(256)
+
+    def call(m, n, k, r, patt, div):
+        d = (C.c_int * max(1, len(div)))(*div)
+        return L.caps_rect_mm_dev(z, z, z, m, n, k, r, patt, d if div else None, None)
+
+    assert call(64, 48, 32, 1, b"b", [2, 2, 1]) == 7
+    assert "BFS" in L.caps_last_cuda_error().decode()
+    assert call(64, 48, 32, 1, b"x", [2, 2, 1]) == 1
+    assert call(64, 48, 32, 2, b"dB", [2, 2, 1, 1, 1, 1]) == 7
+    assert call(64, 48, 32, 1, b"d", [3, 2, 1]) == 2   # 64 % 3
+    assert call(64, 48, 32, 1, b"d", [2, 0, 1]) == 2
+    assert call(0, 48, 32, 0, b"", []) == 2
+    assert call(64, 48, 32, 1, b"d", []) == 8          # no division triples
+
+
+@pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "rect-class", "bench-rect.cpp")),
+                    reason="reference sources absent")
+def test_rect_bench_links_against_library(caps, tmp_path):
+    """The rectangular subproject's own bench-rect.cpp, with its
+    communication / library / sizes objects but without rectmm.o, links
+    against libcaps_gb300.so: its rectMM() call resolves to the library's."""
+    shim = os.path.join(ROOT, "oracle", "ref_shim")
+    ref = os.path.join(REF, "rect-class")
+    libdir = os.path.dirname(caps.LIB_PATH)
+    objs = []
+    for src in ("bench-rect", "communication", "library", "rectsizes", "sizes"):
+        o = str(tmp_path / (src + ".o"))
+        cmd = ["g++", "-O1", "-w", "-fopenmp", "-DNUM_THREADS=1", "-include", os.path.join(shim, "mpi.h"),
+               "-I" + shim, "-I" + ref, "-c", os.path.join(ref, src + ".cpp"), "-o", o]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        assert r.returncode == 0, r.stdout
+        objs.append(o)
+    out = str(tmp_path / "bench-rect")
+    cmd = ["g++", "-fopenmp", "-o", out] + objs + ["-L" + libdir, "-lcaps_gb300", "-Wl,-rpath," + libdir]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout
+    syms = subprocess.run(["nm", out], stdout=subprocess.PIPE, text=True).stdout
+    assert " U _Z6rectMMPdS_S_iiiiiPcPi" in syms  # left to the shared library
