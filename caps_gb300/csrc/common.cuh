@@ -105,15 +105,35 @@ struct LeafTask {
     double *C;
 };
 
+// A DMMA base-case product with the fold of a lean 'd' step that consumes
+// it, done in the GEMM's epilogue on the FP64 accumulator (the same FP64
+// operation the separate combination pass would do on the stored product,
+// so the same bits), per element e with p = (A B)_e:
+//   FOLD_STORE    C = p
+//   FOLD_ADD      C = s0 + p             (EW_ADD with the product second)
+//   FOLD_SUB      C = s0 - p             (EW_SUB)
+//   FOLD_ADD_DUP  C = d1 = s0 + p        (EW_ADD_DUP: U1 into C22 and C12)
+//   FOLD_U2_Q3    C = s0, d1 = s0 + p, d2 = s1 + p  (EW_U2_Q3; s0 = d1, s1 = d2 may alias)
+enum DmmaFold { FOLD_STORE = 0, FOLD_ADD, FOLD_SUB, FOLD_ADD_DUP, FOLD_U2_Q3 };
+struct DmmaTask {
+    const double *A;
+    const double *B;
+    double *C;
+    const double *s0, *s1;
+    double *d1, *d2;
+    int fold;
+    int pad;
+};
+
 // FP64 DMMA GEMM (mma.sync f64): C = A * B for every task, in CTA tiles of
 // one of three shapes (an autotuner axis).
 enum DmmaTile { DMMA_TILE_64x64 = 0, DMMA_TILE_32x32 = 1, DMMA_TILE_128x64 = 2, DMMA_TILES = 3 };
 void dmma_tile_shape(int tile, int *rows, int *cols);
-cudaError_t launch_dmma_gemm(const LeafTask *tasks_dev, int count, int m, cudaStream_t stream,
+cudaError_t launch_dmma_gemm(const DmmaTask *tasks_dev, int count, int m, cudaStream_t stream,
                              int tile = DMMA_TILE_64x64);
 // The same for rectangular leaves: A m x k, B k x n, C m x n (column-major,
 // leading dimensions m, k, m).
-cudaError_t launch_dmma_rect(const LeafTask *tasks_dev, int count, int m, int n, int k, cudaStream_t stream,
+cudaError_t launch_dmma_rect(const DmmaTask *tasks_dev, int count, int m, int n, int k, cudaStream_t stream,
                              int tile = DMMA_TILE_64x64);
 
 // Split form.  Two schemes share one launch sequence; the kernels agree on

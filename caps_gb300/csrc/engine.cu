@@ -238,6 +238,17 @@ static void emit_event(Builder &b, int kind, int index) {
 // give the persistent GEMMs more work units to balance over the SMs.
 static const size_t kSplitGroupBytes = (size_t)16 << 30;
 
+// One batched DMMA launch over m x m leaves, each task with its epilogue fold.
+static void emit_dmma(Builder &b, const std::vector<DmmaTask> &t, int64_t m) {
+    Op o{};
+    o.kind = K_LEAF_DMMA;
+    o.count = (int)t.size();
+    o.m = (int)m;
+    o.tile = b.opt.plain_tile;
+    o.toff = b.table(t);
+    b.ops.push_back(o);
+}
+
 static void emit_leaf_gemm(Builder &b, const std::vector<Prob> &P, int64_t m) {
     if (b.opt.form == CAPS_FORM_SPLIT) {
         // bound split scratch: groups of leaves (the grid's z extent bounds
@@ -273,15 +284,9 @@ static void emit_leaf_gemm(Builder &b, const std::vector<Prob> &P, int64_t m) {
             b.ops.push_back(o);
         }
     } else {
-        std::vector<LeafTask> t;
-        for (const Prob &p : P) t.push_back({p.A, p.B, p.C});
-        Op o{};
-        o.kind = K_LEAF_DMMA;
-        o.count = (int)t.size();
-        o.m = (int)m;
-        o.tile = b.opt.plain_tile;
-        o.toff = b.table(t);
-        b.ops.push_back(o);
+        std::vector<DmmaTask> t;
+        for (const Prob &p : P) t.push_back(DmmaTask{p.A, p.B, p.C, nullptr, nullptr, nullptr, nullptr, FOLD_STORE, 0});
+        emit_dmma(b, t, m);
     }
 }
 
@@ -479,27 +484,77 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
             build(b, {{nd[0].A12, nd[0].B21, Q2top}}, h, nrec - 1, pat + 1);
             emit_event(b, K_WAIT, ev + 2);  // A21, A22, B11, B12, B22
         }
+        // Plain-form leaves right below a step that is not overlapping host
+        // copies: each fold that consumes a product (C22 = C12 = C11 + Q4,
+        // C22 += Q5, the U2 / Q3 triple, C21 -= Q7, C12 += Q6, C11 += Q2) runs
+        // in that product's GEMM epilogue, on the accumulator, instead of as a
+        // pass over the stored product: the same FP64 operations in the same
+        // order, so the same bits, without the product's round trip to HBM.
+        const bool fold = !lead && nrec == 1 && b.opt.form == CAPS_FORM_PLAIN && (b.bs == 1 || b.bs == h);
+        auto folded = [&](int which, int mode) {
+            std::vector<DmmaTask> t;
+            for (const Nd &d : nd) {
+                DmmaTask k{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, mode, 0};
+                switch (which) {
+                    case 2: k.A = d.A12; k.B = d.B21; break;
+                    case 3: case 4: case 5: k.A = d.X; k.B = d.Y; break;
+                    case 6: k.A = d.X; k.B = d.B22; break;
+                    case 7: k.A = d.A22; k.B = d.X; break;
+                }
+                switch (which) {
+                    case 4: k.C = d.C22; k.s0 = d.C11; k.d1 = d.C12; break;                     // ADD_DUP
+                    case 5: k.C = d.C22; k.s0 = d.C22; break;                                   // ADD
+                    case 3: k.C = d.C21; k.s0 = d.C22; k.s1 = d.C12; k.d1 = d.C22; k.d2 = d.C12; break;  // U2_Q3
+                    case 7: k.C = d.C21; k.s0 = d.C21; break;                                   // SUB
+                    case 6: k.C = d.C12; k.s0 = d.C12; break;                                   // ADD
+                    case 2: k.C = d.C11; k.s0 = d.C11; break;                                   // ADD
+                }
+                t.push_back(k);
+            }
+            const long long m3 = (long long)h * h * h * (long long)nd.size();
+            b.adds += m3;
+            b.muls += m3;
+            emit_dmma(b, t, h);
+        };
         form(EW_FORM_T4S4);
-        sub(4);
-        comb(EW_ADD_DUP, [](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = d.Q; t.dst[0] = d.C22; t.dst[1] = d.C12; });
+        if (fold) {
+            folded(4, FOLD_ADD_DUP);
+        } else {
+            sub(4);
+            comb(EW_ADD_DUP, [](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = d.Q; t.dst[0] = d.C22; t.dst[1] = d.C12; });
+        }
         if (lead) {
             comb(EW_ADD, [&](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = Q2top; t.dst[0] = d.C11; });
             if (top) emit_event(b, K_RECORD, EV_C_FIRST);  // C11 final
         }
         form(EW_FORM_T5S5);
-        sub(5);
-        comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C22; t.src[1] = d.Q; t.dst[0] = d.C22; });
+        if (fold) {
+            folded(5, FOLD_ADD);
+        } else {
+            sub(5);
+            comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C22; t.src[1] = d.Q; t.dst[0] = d.C22; });
+        }
         form(EW_FORM_T3S3);
-        sub(3);
-        comb(EW_U2_Q3, [](const Nd &d, EwTask &t) { t.src[0] = d.C22; t.src[1] = d.C12; t.src[2] = d.Q; t.dst[0] = d.C21; t.dst[1] = d.C22; t.dst[2] = d.C12; });
+        if (fold) {
+            folded(3, FOLD_U2_Q3);
+        } else {
+            sub(3);
+            comb(EW_U2_Q3, [](const Nd &d, EwTask &t) { t.src[0] = d.C22; t.src[1] = d.C12; t.src[2] = d.Q; t.dst[0] = d.C21; t.dst[1] = d.C22; t.dst[2] = d.C12; });
+        }
         if (top) emit_event(b, K_RECORD, EV_C_FIRST + 1);  // C22 final
         form(EW_FORM_S7);
-        sub(7);
-        comb(EW_SUB, [](const Nd &d, EwTask &t) { t.src[0] = d.C21; t.src[1] = d.Q; t.dst[0] = d.C21; });
+        if (fold) {
+            folded(7, FOLD_SUB);
+        } else {
+            sub(7);
+            comb(EW_SUB, [](const Nd &d, EwTask &t) { t.src[0] = d.C21; t.src[1] = d.Q; t.dst[0] = d.C21; });
+        }
         if (top) emit_event(b, K_RECORD, EV_C_FIRST + 2);  // C21 final
         form(EW_FORM_T6);
-        sub(6);
-        if (top) {
+        if (fold) {
+            folded(6, FOLD_ADD);
+        } else if (top) {
+            sub(6);
             // C12 = U3 + Q6 in parts, each recorded when final
             for (int k = 0; k < C12_PARTS; k++) {
                 const int64_t p0 = c12_part_begin(q, k), p1 = c12_part_begin(q, k + 1);
@@ -508,9 +563,12 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
                 emit_event(b, K_RECORD, EV_C_FIRST + 3 + k);
             }
         } else {
+            sub(6);
             comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C12; t.src[1] = d.Q; t.dst[0] = d.C12; });
         }
-        if (!lead) {
+        if (fold) {
+            folded(2, FOLD_ADD);
+        } else if (!lead) {
             sub(2);
             comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C11; t.src[1] = d.Q; t.dst[0] = d.C11; });
         }
@@ -701,7 +759,7 @@ static caps_status launch_ops(const std::vector<Op> &ops, char *tables, char *ws
                 break;
             case K_LEAF_DMMA:
                 if (timed) ev_begin(r.e0);
-                err = launch_dmma_gemm(reinterpret_cast<const LeafTask *>(tables + o.toff), o.count, o.m, s, o.tile);
+                err = launch_dmma_gemm(reinterpret_cast<const DmmaTask *>(tables + o.toff), o.count, o.m, s, o.tile);
                 r.phase = PH_MUL;
                 r.gemm = true;
                 r.m3 = (double)o.count * o.m * (double)o.m * o.m;
@@ -1564,14 +1622,15 @@ static caps_status rect_mm_locked(const double *A, const double *B, double *C, i
     std::vector<uint8_t> blob;
     for (size_t i = 0; i < walk.size(); i++) {
         if (last[walk[i].C] != i) continue;
-        const uint8_t *p = reinterpret_cast<const uint8_t *>(&walk[i]);
-        blob.insert(blob.end(), p, p + sizeof(LeafTask));
+        const DmmaTask t{walk[i].A, walk[i].B, walk[i].C, nullptr, nullptr, nullptr, nullptr, FOLD_STORE, 0};
+        const uint8_t *p = reinterpret_cast<const uint8_t *>(&t);
+        blob.insert(blob.end(), p, p + sizeof(DmmaTask));
     }
-    const int count = (int)(blob.size() / sizeof(LeafTask));
+    const int count = (int)(blob.size() / sizeof(DmmaTask));
     CAPS_TRY(ensure(g_rect, blob.size()));
     CAPS_TRY(upload_tables(blob, g_rect.ptr, s));
     long long l0 = g_launches;
-    CAPS_CUDA_TRY(launch_dmma_rect(reinterpret_cast<const LeafTask *>(g_rect.ptr), count, (int)leaf[0], (int)leaf[1],
+    CAPS_CUDA_TRY(launch_dmma_rect(reinterpret_cast<const DmmaTask *>(g_rect.ptr), count, (int)leaf[0], (int)leaf[1],
                                    (int)leaf[2], s));
     g_counters = caps_counters();
     g_counters.multiplications = (long long)count * leaf[0] * leaf[1] * leaf[2];

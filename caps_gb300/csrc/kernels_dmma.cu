@@ -14,7 +14,8 @@
 // Three shapes (caps_dmma_tile): 64 x 64 (2 x 2 warps, the default),
 // 32 x 32 (one warp: four times the CTAs, for small leaves) and 128 x 64
 // (4 x 2 warps: half the B traffic per multiply-add).  The autotuner times
-// them per size.
+// them per size.  The epilogue applies the task's fold (DmmaFold) of the
+// lean 'd' step that consumes the product.
 #include "common.cuh"
 
 namespace caps {
@@ -31,13 +32,13 @@ __device__ __forceinline__ void dmma_8x8x4(double (&d)[2], double a, double b) {
 }  // namespace
 
 template <int WM, int WN>
-__global__ void __launch_bounds__(32 * WM * WN) dmma_gemm_kernel(const LeafTask *__restrict__ tasks, int m, int n,
+__global__ void __launch_bounds__(32 * WM * WN) dmma_gemm_kernel(const DmmaTask *__restrict__ tasks, int m, int n,
                                                                  int k) {
     constexpr int BM = 32 * WM, BN = 32 * WN, NT = 32 * WM * WN;
     constexpr int LDA = BM + 8, LDB = BN + 8;  // padded rows (banks)
     __shared__ double As[BK][LDA];  // As[k][i]
     __shared__ double Bs[BK][LDB];  // Bs[k][j]
-    const LeafTask t = tasks[blockIdx.z];
+    const DmmaTask t = tasks[blockIdx.z];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int wr = warp / WN, wc = warp % WN;
     const int64_t i0 = (int64_t)blockIdx.y * BM, j0 = (int64_t)blockIdx.x * BN;
@@ -88,12 +89,32 @@ __global__ void __launch_bounds__(32 * WM * WN) dmma_gemm_kernel(const LeafTask 
             for (int e = 0; e < 2; e++) {
                 const int64_t gi = i0 + 32 * wr + 8 * a + (lane >> 2);
                 const int64_t gj = j0 + 32 * wc + 8 * b + 2 * (lane & 3) + e;
-                if (gi < M && gj < N) t.C[gi + gj * M] = acc[a][b][e];
+                if (gi >= M || gj >= N) continue;
+                const int64_t x = gi + gj * M;
+                const double p = acc[a][b][e];
+                switch (t.fold) {
+                    case FOLD_ADD: t.C[x] = t.s0[x] + p; break;
+                    case FOLD_SUB: t.C[x] = t.s0[x] - p; break;
+                    case FOLD_ADD_DUP: {
+                        const double v = t.s0[x] + p;
+                        t.C[x] = v;
+                        t.d1[x] = v;
+                        break;
+                    }
+                    case FOLD_U2_Q3: {
+                        const double u2 = t.s0[x], u1 = t.s1[x];
+                        t.C[x] = u2;
+                        t.d1[x] = u2 + p;
+                        t.d2[x] = u1 + p;
+                        break;
+                    }
+                    default: t.C[x] = p;
+                }
             }
 }
 
 template <int WM, int WN>
-static cudaError_t launch_dmma_shape(const LeafTask *tasks_dev, int count, int m, int n, int k, cudaStream_t stream) {
+static cudaError_t launch_dmma_shape(const DmmaTask *tasks_dev, int count, int m, int n, int k, cudaStream_t stream) {
     const unsigned rows = (unsigned)((m + 32 * WM - 1) / (32 * WM)), cols = (unsigned)((n + 32 * WN - 1) / (32 * WN));
     for (int base = 0; base < count; base += 65535) {
         const int c = count - base < 65535 ? count - base : 65535;
@@ -112,7 +133,7 @@ void dmma_tile_shape(int tile, int *rows, int *cols) {
     }
 }
 
-cudaError_t launch_dmma_rect(const LeafTask *tasks_dev, int count, int m, int n, int k, cudaStream_t stream,
+cudaError_t launch_dmma_rect(const DmmaTask *tasks_dev, int count, int m, int n, int k, cudaStream_t stream,
                              int tile) {
     if (count <= 0 || m <= 0 || n <= 0) return cudaSuccess;
     switch (tile) {
@@ -122,7 +143,7 @@ cudaError_t launch_dmma_rect(const LeafTask *tasks_dev, int count, int m, int n,
     }
 }
 
-cudaError_t launch_dmma_gemm(const LeafTask *tasks_dev, int count, int m, cudaStream_t stream, int tile) {
+cudaError_t launch_dmma_gemm(const DmmaTask *tasks_dev, int count, int m, cudaStream_t stream, int tile) {
     return launch_dmma_rect(tasks_dev, count, m, m, m, stream, tile);
 }
 

@@ -344,3 +344,31 @@ def test_host_entry_hybrid_top_step(caps, oracle_mod, cuda, k):
         c = np.full(n * n, np.nan)
         caps.multiply(a, b, c, caps.MatDescriptor.make(n, r, 1, k), "hbd", form=form)
         assert np.array_equal(mat_of(oracle_mod, c, n, r), (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64))
+
+
+@pytest.mark.parametrize("n,r,pat,ref_pat", [(1024, 2, "dd", "bb"), (1024, 3, "ddd", "bbb"), (896, 2, "bd", "bb"),
+                                             (448, 1, "d", "b"), (1024, 3, "bdd", "bbb")])
+def test_plain_d_step_epilogue_folds_bit_identical_to_b(caps, oracle_mod, cuda, n, r, pat, ref_pat):
+    """A lean 'd' step over plain-form leaves folds its combinations into the
+    products' DMMA epilogues (C22 = C12 = C11 + Q4, C22 += Q5, the U2 / Q3
+    triple, C21 -= Q7, C12 += Q6, C11 += Q2).  They are the reference's FP64
+    operations in its order, as calcCij does them for a 'b' step, so the two
+    results agree bit for bit on float data; the fold launches no combination
+    pass of its own."""
+    import torch
+    rng = np.random.default_rng(n + r)
+    A = rng.uniform(-1, 1, (n, n))
+    B = rng.uniform(-1, 1, (n, n))
+    dA = torch.from_numpy(caps_of(oracle_mod, A, r)).to(cuda)
+    dB = torch.from_numpy(caps_of(oracle_mod, B, r)).to(cuda)
+    out, launches = {}, {}
+    for p in (pat, ref_pat):
+        dC = torch.full_like(dA, float("nan"))
+        caps.multiply(dA, dB, dC, caps.MatDescriptor.make(n, r), p, form="plain")
+        torch.cuda.synchronize()
+        out[p] = dC.cpu().numpy()
+        launches[p] = caps.counters()["kernel_launches"]
+    assert np.array_equal(out[pat], out[ref_pat])
+    if pat == "d":
+        # one 'd' step over 7 leaves: 5 operand-sum launches and 7 products, no folds
+        assert launches[pat] == 5 + 7
