@@ -419,7 +419,23 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
             double *W = b.alloc(3 * q);
             d.X = W; d.Y = W + q; d.Q = W + 2 * q;
         }
+        // A step overlapping host copies (below) forms all eight operand sums
+        // in one pass once every input is in, into ST = T3 T4 T5 T6 S3 S4 S5
+        // S7 (the same formulas as the lean passes: the same bits), and each
+        // form() then only points X, Y at its pair.
+        double *ST = nullptr;
         auto form = [&](int op) {
+            if (ST) {
+                Nd &d = nd[0];
+                switch (op) {
+                    case EW_FORM_T4S4: d.X = ST + q; d.Y = ST + 5 * q; break;
+                    case EW_FORM_T5S5: d.X = ST + 2 * q; d.Y = ST + 6 * q; break;
+                    case EW_FORM_T3S3: d.X = ST; d.Y = ST + 4 * q; break;
+                    case EW_FORM_S7: d.X = ST + 7 * q; break;
+                    case EW_FORM_T6: d.X = ST + 3 * q; break;
+                }
+                return;
+            }
             std::vector<EwTask> t(nd.size());
             for (size_t i = 0; i < nd.size(); i++) {
                 const Nd &d = nd[i];
@@ -483,6 +499,12 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
             emit_event(b, K_WAIT, ev + 1);  // A12, B21
             build(b, {{nd[0].A12, nd[0].B21, Q2top}}, h, nrec - 1, pat + 1);
             emit_event(b, K_WAIT, ev + 2);  // A21, A22, B11, B12, B22
+            ST = b.alloc(8 * q);
+            const Nd &d = nd[0];
+            emit_ew(b, EW_FORM_ST,
+                    {EwTask{{d.A11, d.A21, d.A12, d.A22, d.B11, d.B21, d.B12, d.B22},
+                            {ST, ST + q, ST + 2 * q, ST + 3 * q, ST + 4 * q, ST + 5 * q, ST + 6 * q, ST + 7 * q}}},
+                    q);
         }
         // Plain-form leaves right below a step that is not overlapping host
         // copies: each fold that consumes a product (C22 = C12 = C11 + Q4,

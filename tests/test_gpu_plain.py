@@ -372,3 +372,24 @@ def test_plain_d_step_epilogue_folds_bit_identical_to_b(caps, oracle_mod, cuda, 
     if pat == "d":
         # one 'd' step over 7 leaves: 5 operand-sum launches and 7 products, no folds
         assert launches[pat] == 5 + 7
+
+
+@pytest.mark.parametrize("form", ["plain", "split"])
+@pytest.mark.parametrize("n,r", [(1024, 3), (512, 2), (256, 1)])
+def test_host_entry_float_bit_identical_to_device(caps, oracle_mod, cuda, form, n, r):
+    """The host entry point's overlapped plan (a lean top step, its first
+    subproduct a lean step on sub-quadrants, the operand sums formed in one
+    pass once every input is in, C12 in four parts) computes the same FP64
+    operations in the same order as the device entry point's 'b' steps:
+    float results agree bit for bit."""
+    import torch
+    rng = np.random.default_rng(n + r + len(form))
+    a = caps_of(oracle_mod, rng.uniform(-1, 1, (n, n)), r)
+    b = caps_of(oracle_mod, rng.uniform(-1, 1, (n, n)), r)
+    c = np.full(n * n, np.nan)
+    caps.multiply(a, b, c, caps.MatDescriptor.make(n, r), None, form=form)
+    dC = torch.full((n * n,), float("nan"), dtype=torch.float64, device=cuda)
+    caps.multiply(torch.from_numpy(a).to(cuda), torch.from_numpy(b).to(cuda), dC, caps.MatDescriptor.make(n, r),
+                  "b" * r, form=form)
+    torch.cuda.synchronize()
+    assert np.array_equal(c, dC.cpu().numpy())
