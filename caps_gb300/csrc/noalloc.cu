@@ -21,8 +21,7 @@
 //     calls from several host threads, and calls beside the library's other
 //     entry points, take turns on the host;
 //   - the first call on a device resolves the array's device address
-//     (cudaGetSymbolAddress) with that device current.  Make that first call
-//     before any stream capture is begun on the device;
+//     (cudaGetSymbolAddress) with that device current, and keeps it;
 //   - every call reads the kernels' status word back, so it synchronises the
 //     stream it is given before returning.
 #include "common.cuh"

@@ -143,8 +143,8 @@ caps_status caps_leaf_gemm_dev(const double *A, const double *B, double *C, int 
  * slices / diagonals as in caps_options (0 = automatic).  All calls share
  * the array, so calls that overlap on the GPU race: serialise them.  The
  * first call on a device looks up the array's address with that device
- * current; make it before any stream capture begins.  Synchronises
- * `stream` before returning (it reads the kernels' status word back). */
+ * current and keeps it.  Synchronises `stream` before returning (it reads
+ * the kernels' status word back). */
 caps_status caps_leaf_gemm_split_noalloc_dev(const double *A, const double *B, double *C, int m,
                                              int slices, int diagonals, void *stream);
 
