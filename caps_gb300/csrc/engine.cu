@@ -509,9 +509,12 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
         // Plain-form leaves right below a step that is not overlapping host
         // copies: each fold that consumes a product (C22 = C12 = C11 + Q4,
         // C22 += Q5, the U2 / Q3 triple, C21 -= Q7, C12 += Q6, C11 += Q2) runs
-        // in that product's GEMM epilogue, on the accumulator, instead of as a
+        // in that product's DMMA epilogue, on the accumulator, instead of as a
         // pass over the stored product: the same FP64 operations in the same
         // order, so the same bits, without the product's round trip to HBM.
+        // (Split-form leaves keep the passes: in the residue GEMM's
+        // reconstruction warps the folds' FP64 adds slowed the GEMM more than
+        // the passes cost.)
         const bool fold = !lead && nrec == 1 && b.opt.form == CAPS_FORM_PLAIN && (b.bs == 1 || b.bs == h);
         auto folded = [&](int which, int mode) {
             std::vector<DmmaTask> t;

@@ -327,3 +327,30 @@ def test_first_split_call_of_a_process_runs_residues(caps, cuda):
     assert out.returncode == 0, out.stdout
     first, second = (int(x) for x in out.stdout.strip().splitlines()[-1].split())
     assert first == second > 0, out.stdout
+
+
+@pytest.mark.parametrize("n,r,pat,ref_pat,wide", [(1024, 2, "dd", "bb", False), (896, 2, "bd", "bb", True),
+                                                  (2048, 2, "dd", "bb", True), (512, 1, "d", "b", False)])
+def test_split_d_step_bit_identical_to_b(caps, oracle_mod, cuda, n, r, pat, ref_pat, wide):
+    """A lean 'd' step over residue-scheme leaves combines its products with
+    the reference's FP64 operations in its order (C22 = C12 = C11 + Q4,
+    C22 += Q5, the U2 / Q3 triple, C21 -= Q7, C12 += Q6, C11 += Q2), as
+    calcCij does for a 'b' step, so the two agree bit for bit on float data,
+    wide-range data included."""
+    import torch
+    rng = np.random.default_rng(7 * n + r)
+    A = rng.uniform(-1, 1, (n, n))
+    B = rng.uniform(-1, 1, (n, n))
+    if wide:
+        A *= 2.0 ** rng.integers(-20, 21, (n, n))
+        B *= 2.0 ** rng.integers(-20, 21, (n, n))
+    dA = torch.from_numpy(caps_of(oracle_mod, A, r)).to(cuda)
+    dB = torch.from_numpy(caps_of(oracle_mod, B, r)).to(cuda)
+    out = {}
+    for p in (pat, ref_pat):
+        dC = torch.full_like(dA, float("nan"))
+        caps.multiply(dA, dB, dC, caps.MatDescriptor.make(n, r), p, form="split")
+        torch.cuda.synchronize()
+        assert caps.counters()["split_moduli"] > 0  # the residues ran
+        out[p] = dC.cpu().numpy()
+    assert np.array_equal(out[pat], out[ref_pat])
