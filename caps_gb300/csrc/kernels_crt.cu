@@ -136,14 +136,54 @@ struct Limbs {
     float a[4];
 };
 
-__device__ __forceinline__ Limbs limbs14(long long X) {
-    const unsigned long long OFF = 0x0080020008002000ull;  // 8192 * sum_{k<4} 16384^k
-    const unsigned long long U = (unsigned long long)X + OFF;
+// The limbs of X = round(x 2^f) (ties to even; scaled_round in
+// split_common.cuh computes the same X), on 32-bit operations: from the two
+// halves of x's encoding (M 2^e, M below 2^53), q = M shifted by e + f, then
+// the base-16384 digits of X + 8192 (1 + 2^14 + 2^28 + 2^42) less 8192.  For
+// the slicer's f (t - E with E the row's exponent bound, t <= 55) the shift
+// e + f is at most 3.  Rounding right by r: q = M >> r, plus one when the bit
+// below q is set and a lower bit is set or q is odd.  Checked equal to the
+// 64-bit formulation on 40 million doubles and shifts, ties, subnormals and
+// zeros included; it takes fewer integer instructions.
+__device__ __forceinline__ Limbs scaled_limbs14(double x, int f) {
+    const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
+    const int field = (int)((hi >> 20) & 0x7FFu);
+    const uint32_t mh = (hi & 0xFFFFFu) | (field ? 0x100000u : 0u);
+    const int sh = (field ? field - 1075 : -1074) + f;
+    uint32_t ql, qh;
+    if (sh >= 0) {  // at most 3
+        ql = lo << sh;
+        qh = __funnelshift_l(lo, mh, sh);
+    } else if (sh >= -53) {
+        const int r1 = -sh - 1;  // 0..52: M >> r1 ends in the round bit
+        uint32_t tl, th;
+        bool sticky;             // any bit below the round bit
+        if (r1 < 32) {
+            tl = __funnelshift_r(lo, mh, r1);
+            th = mh >> r1;
+            sticky = ((lo << (31 - r1)) << 1) != 0u;
+        } else {
+            tl = mh >> (r1 - 32);
+            th = 0u;
+            sticky = lo != 0u || ((mh << (63 - r1)) << 1) != 0u;
+        }
+        ql = __funnelshift_r(tl, th, 1);
+        qh = th >> 1;
+        const uint32_t up = tl & ((sticky ? 1u : 0u) | ql) & 1u;
+        ql += up;
+        qh += ql < up ? 1u : 0u;
+    } else {        // |x 2^f| < 1/2
+        ql = qh = 0u;
+    }
+    const uint64_t q = ((uint64_t)qh << 32) | ql;
+    const uint64_t OFF = 0x0080020008002000ull;  // 8192 * sum_{k<4} 16384^k
+    const uint64_t U = (hi >> 31) ? OFF - q : OFF + q;
+    const uint32_t ul = (uint32_t)U, uh = (uint32_t)(U >> 32);
     Limbs l;
-    l.a[0] = small_int_to_float((int)(U & 16383u) - 8192);
-    l.a[1] = small_int_to_float((int)((U >> 14) & 16383u) - 8192);
-    l.a[2] = small_int_to_float((int)((U >> 28) & 16383u) - 8192);
-    l.a[3] = small_int_to_float((int)(U >> 42) - 8192);
+    l.a[0] = small_int_to_float((int)(ul & 16383u) - 8192);
+    l.a[1] = small_int_to_float((int)((ul >> 14) & 16383u) - 8192);
+    l.a[2] = small_int_to_float((int)(__funnelshift_r(ul, uh, 28) & 16383u) - 8192);
+    l.a[3] = small_int_to_float((int)(uh >> 10) - 8192);
     return l;
 }
 
@@ -305,7 +345,7 @@ __device__ __forceinline__ void crt_slice_tile(const LeafTask *__restrict__ task
     for (int e = 0; e < 8; e++) v[e] = (live && k0 + e < M) ? __ldg(src + e * sk) : 0.0;
     Limbs x[8];
 #pragma unroll
-    for (int e = 0; e < 8; e++) x[e] = limbs14(scaled_round(v[e], f));
+    for (int e = 0; e < 8; e++) x[e] = scaled_limbs14(v[e], f);
     switch (L) {
         // float data need 17 moduli at 55 bits, 16 or 15 under an operand-bit
         // cap: unrolled, the FMAs take their constants straight from the
