@@ -61,11 +61,12 @@ def parse():
     ap.add_argument("--no-wide", action="store_true", help="skip the wide-range (u*2^k) error check")
     ap.add_argument("--samples", type=int, default=256, help="entries checked against binary128")
     ap.add_argument("--workload", default="split16384",
-                    choices=["split16384", "plain8192", "batched512", "int32768", "chol16384"],
+                    choices=["split16384", "plain8192", "batched512", "int32768", "chol16384", "rect"],
                     help="split16384: the headline (n=16384, r=3, split vs FP64); plain8192: FP64 Strassen "
                          "n=8192 r=3 'ddd'; batched512: 512 uneven multiplies; int32768: n=32768 r=4 'bbdd' "
                          "integers under a 120 GB budget; chol16384: the Cholesky subproject's update "
-                         "C = C - A B^T, n=16384, r=3")
+                         "C = C - A B^T, n=16384, r=3; rect: the rectangular subproject's rectMM, "
+                         "16384 x 8192 times 8192 x 12288, r=2 'dd'")
     return ap.parse_args()
 
 
@@ -345,6 +346,84 @@ def run_plain8192(args, world, rank, local):
                                      gpu_launches=cg.counters()["kernel_launches"] * args.steps)), flush=True)
 
 
+def run_rect(args, world, rank, local):
+    """The rectangular subproject's rectMM on one rank (rect-class/rectmm.cpp):
+    A 16384 x 8192 times B 8192 x 12288, r = 2 'dd', divisions (2,1,1)(1,3,1):
+    six base products of 8192 x 8192 by 8192 x 4096 on FP64 DMMA, the whole
+    product (every divk is 1, and divm or divn is 1 at each level)."""
+    import numpy as np
+    import torch
+    import caps_gb300 as cg
+    from fractions import Fraction
+    dev = torch.device("cuda", local)
+    m, n, k, r, patt, div = 16384, 12288, 8192, 2, "dd", [2, 1, 1, 1, 3, 1]
+    g = torch.Generator(device=dev)
+    g.manual_seed(41 + rank)
+    A = torch.rand(m * k, dtype=torch.float64, device=dev, generator=g) * 2 - 1
+    B = torch.rand(k * n, dtype=torch.float64, device=dev, generator=g) * 2 - 1
+    C = torch.zeros(m * n, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(max(args.warmup, 3)):
+        cg.rect_mm(A, B, C, m, n, k, r, patt, div, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    launches = cg.counters()["kernel_launches"]
+    barrier(world)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            cg.rect_mm(A, B, C, m, n, k, r, patt, div, stream=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    t = max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps, world)
+    if rank != 0:
+        return
+    # the layout: A rows in two column-major halves, B column-major, C in
+    # (row half, column third) blocks of 8192 x 4096, column-major
+    hA, hB, hC = A.cpu().numpy(), B.cpu().numpy(), C.cpu().numpy()
+    rng = np.random.default_rng(5)
+    worst = 0.0
+    for _ in range(16):
+        i, j = int(rng.integers(0, m)), int(rng.integers(0, n))
+        ai = hA[(i // 8192) * 8192 * k:][: 8192 * k].reshape(k, 8192)[:, i % 8192]
+        bj = hB[j * k:(j + 1) * k]
+        cij = hC[((i // 8192) * 3 + j // 4096) * 8192 * 4096 + (j % 4096) * 8192 + i % 8192]
+        exact = sum(Fraction(float(a)) * Fraction(float(b)) for a, b in zip(ai, bj))
+        absdot = float(np.abs(ai) @ np.abs(bj))
+        worst = max(worst, abs(float(Fraction(float(cij)) - exact)) / absdot)
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle
+        cores = os.cpu_count() or 1
+        oracle.build()
+        blas = oracle.use_blas(True, threads=cores)
+        oracle.set_threads(cores)
+        try:
+            tc0 = time.perf_counter()
+            oracle.rect_mm(hA, hB, hC, m, n, k, r, patt, div)
+            tcpu = time.perf_counter() - tc0
+        finally:
+            oracle.use_blas(False)
+        cpu = {"value": 2.0 * m * n * k / tcpu / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+               "sample": "one whole rectMM of the same shape: the oracle's restatement of the one-rank walk, "
+                         "%s dgemm at the base blocks, %d threads (%.2f s)" % ("OpenBLAS" if blas else "loop",
+                                                                                cores, tcpu)}
+    flops = 2.0 * m * n * k
+    peak = 1.13  # the FP64 pipe's rate at 2.07 GHz, from the DMMA capture (profiles/dmma_gemm_kernel_n4096.md)
+    print(json.dumps(common_line(
+        "effective TFLOP/s (2mnk/t), rectMM 16384x8192 * 8192x12288, r=2 'dd'", world * flops / t / 1e12, args,
+        world, t * 1e3,
+        {"workload": "the rectangular subproject's rectMM on one rank, m=16384 n=12288 k=8192, r=2 'dd', "
+                     "divisions (2,1,1)(1,3,1), FP64 DMMA base case", "m": m, "n": n, "k": k, "nrec": r,
+         "pattern": patt, "divisions": div, "inputs": "uniform[-1,1) seeded (torch.Generator)"},
+        error={"max_elementwise_rel": worst, "samples": 16, "reference": "exact rational dot products"},
+        roofline={"bound": "tensor", "kernel": "dmma_gemm_kernel", "achieved": flops / t / 1e12, "peak": peak,
+                  "unit": "TFLOP/s", "frac": flops / t / 1e12 / peak,
+                  "peak_source": "FP64 (DMMA) pipe rate at 2.07 GHz, from profiles/dmma_gemm_kernel_n4096.md",
+                  "traffic": None},
+        cpu_baseline=cpu, gpu_launches=launches * args.steps, clocks=clk.summary())), flush=True)
+
+
 def run_batched512(args, world, rank, local):
     """512 independent multiplies, n log-uniform over {448, 896, 1792, 3584}."""
     import numpy as np
@@ -610,7 +689,7 @@ def main():
         if not os.path.exists(cbuild.LIB):
             cbuild.build()
         {"plain8192": run_plain8192, "batched512": run_batched512, "int32768": run_int32768,
-         "chol16384": run_chol16384}[args.workload](
+         "chol16384": run_chol16384, "rect": run_rect}[args.workload](
             args, world, rank, local)
         if world > 1:
             import torch.distributed as dist
