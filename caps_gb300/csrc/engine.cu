@@ -133,7 +133,10 @@ constexpr int EV_C_FIRST = 3;  // events 3..5: C11, C22, C21 final; 6..9: the pa
 // EV_INNER (A11's and B11's first sub-quadrants), +1 (A11's 12 and B11's 21),
 // +2 (the rest of A11 and B11).
 constexpr int EV_INNER = 6 + C12_PARTS;
-constexpr int HOST_EVENTS = EV_INNER + 3;
+// The top step's Q5 = T5 S5 needs A11, A21, B12 and B22 only: it runs once
+// A21, B12 and B22 are in (event EV_Q5), before A22, the last copy.
+constexpr int EV_Q5 = EV_INNER + 3;
+constexpr int HOST_EVENTS = EV_Q5 + 1;
 
 // Part k of C12's q elements: [c12_part_begin(q, k), c12_part_begin(q, k + 1)),
 // boundaries on even elements so that the parts keep 16-byte alignment.
@@ -495,12 +498,22 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
             b.overlap_stage = 2;                  // below this step: no waits
             sub(1);
         }
+        double *Q5top = nullptr;
         if (lead) {
             emit_event(b, K_WAIT, ev + 1);  // A12, B21
             build(b, {{nd[0].A12, nd[0].B21, Q2top}}, h, nrec - 1, pat + 1);
-            emit_event(b, K_WAIT, ev + 2);  // A21, A22, B11, B12, B22
             ST = b.alloc(8 * q);
             const Nd &d = nd[0];
+            if (top) {
+                // Q5 = T5 S5 before A22 is in: T5 = A11 - A21, S5 = B22 - B12
+                emit_event(b, K_WAIT, EV_Q5);  // A21, B12, B22
+                emit_ew(b, EW_FORM_T5S5,
+                        {EwTask{{d.A11, d.A21, d.A12, d.A22, d.B11, d.B21, d.B12, d.B22}, {ST + 2 * q, ST + 6 * q}}},
+                        q);
+                Q5top = b.alloc(q);
+                build(b, {{ST + 2 * q, ST + 6 * q, Q5top}}, h, nrec - 1, pat + 1);
+            }
+            emit_event(b, K_WAIT, ev + 2);  // every input
             emit_ew(b, EW_FORM_ST,
                     {EwTask{{d.A11, d.A21, d.A12, d.A22, d.B11, d.B21, d.B12, d.B22},
                             {ST, ST + q, ST + 2 * q, ST + 3 * q, ST + 4 * q, ST + 5 * q, ST + 6 * q, ST + 7 * q}}},
@@ -555,6 +568,8 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
         form(EW_FORM_T5S5);
         if (fold) {
             folded(5, FOLD_ADD);
+        } else if (Q5top) {
+            comb(EW_ADD, [&](const Nd &d, EwTask &t) { t.src[0] = d.C22; t.src[1] = Q5top; t.dst[0] = d.C22; });
         } else {
             sub(5);
             comb(EW_ADD, [](const Nd &d, EwTask &t) { t.src[0] = d.C22; t.src[1] = d.Q; t.dst[0] = d.C22; });
@@ -1737,7 +1752,7 @@ caps_status caps_multiply_host(const double *A, const double *B, double *C, caps
     // The input copies, enqueued once the plan's tables are queued on s (a
     // copy queued later on s waits behind these in the host-to-device copy
     // engine).  Quadrants X11, X21, X12, X22 at 0, q, 2q, 3q: A11 + B11 (Q1),
-    // then A12 + B21 (Q2), then the rest.
+    // then A12 + B21 (Q2), then A21, B12, B22 (Q5), then A22.
     // With two or more levels the plan's Q1 waits on the sub-quadrants of A11
     // and B11 (events EV_INNER..+2): 11 and 11, then 12 and 21, then the rest.
     const bool inner = desc.nrec >= 2;
@@ -1770,10 +1785,11 @@ caps_status caps_multiply_host(const double *A, const double *B, double *C, caps
         CAPS_CUDA_TRY(h2d(dA, A, 2));
         CAPS_CUDA_TRY(h2d(dB, B, 1));
         CAPS_CUDA_TRY(cudaEventRecord(g_host_events[1], cs));
-        CAPS_CUDA_TRY(h2d(dA, A, 1));
-        CAPS_CUDA_TRY(h2d(dA, A, 3));
+        CAPS_CUDA_TRY(h2d(dA, A, 1));  // A21, B12, B22: Q5's inputs
         CAPS_CUDA_TRY(h2d(dB, B, 2));
         CAPS_CUDA_TRY(h2d(dB, B, 3));
+        CAPS_CUDA_TRY(cudaEventRecord(g_host_events[EV_Q5], cs));
+        CAPS_CUDA_TRY(h2d(dA, A, 3));  // A22 last
         CAPS_CUDA_TRY(cudaEventRecord(g_host_events[2], cs));
         if (timeline) CAPS_CUDA_TRY(cudaEventRecord(hs->timing[2], cs));
         return CAPS_OK;
