@@ -179,6 +179,8 @@ struct Builder {
     int split_group = 0;
     bool host_overlap = false;  // emit K_WAIT / K_RECORD at the top-level 'd' step
     int overlap_stage = 0;      // 0: top step not built yet; 1: building its Q1; 2: no more waits
+    bool overlap_extras = true; // the overlapped top step's one-pass sums and early Q5 (about
+                                // 10 quarter buffers more; dropped when the budget is short)
     int hybrid = 1;             // subproducts an 'h' step runs at once (desc.nproc_summa)
 
     size_t mark() const { return top; }
@@ -502,6 +504,8 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
         if (lead) {
             emit_event(b, K_WAIT, ev + 1);  // A12, B21
             build(b, {{nd[0].A12, nd[0].B21, Q2top}}, h, nrec - 1, pat + 1);
+        }
+        if (lead && b.overlap_extras) {
             ST = b.alloc(8 * q);
             const Nd &d = nd[0];
             if (top) {
@@ -518,6 +522,8 @@ static void build(Builder &b, const std::vector<Prob> &P, int64_t n, int nrec, c
                     {EwTask{{d.A11, d.A21, d.A12, d.A22, d.B11, d.B21, d.B12, d.B22},
                             {ST, ST + q, ST + 2 * q, ST + 3 * q, ST + 4 * q, ST + 5 * q, ST + 6 * q, ST + 7 * q}}},
                     q);
+        } else if (lead) {
+            emit_event(b, K_WAIT, ev + 2);  // every input; the lean passes form the sums
         }
         // Plain-form leaves right below a step that is not overlapping host
         // copies: each fold that consumes a product (C22 = C12 = C11 + Q4,
@@ -701,9 +707,10 @@ struct Planned {
 
 static caps_status plan(const double *A, const double *B, double *C, const caps_desc &d,
                         const char *pat, const caps_options &o, char *ws_base, Planned &pl,
-                        bool host_overlap = false) {
+                        bool host_overlap = false, bool overlap_extras = true) {
     pl.b = Builder();
     pl.b.host_overlap = host_overlap;
+    pl.b.overlap_extras = overlap_extras;
     pl.b.ws_base = ws_base;
     pl.b.bs = d.bs;
     pl.b.hybrid = d.nproc_summa;
@@ -940,14 +947,19 @@ static caps_status multiply_dev_locked(const double *A, const double *B, double 
         auto_pattern(d, o, pat);
     }
     Planned pl;
-    CAPS_TRY(plan(A, B, C, d, pat, o, nullptr, pl, host_overlap));
+    bool extras = true;
+    CAPS_TRY(plan(A, B, C, d, pat, o, nullptr, pl, host_overlap, extras));
+    if (host_overlap && o.workspace_limit > 0 && (long long)pl.ws_bytes > o.workspace_limit) {
+        extras = false;  // the overlapped top step without its extra buffers
+        CAPS_TRY(plan(A, B, C, d, pat, o, nullptr, pl, host_overlap, extras));
+    }
     if (o.workspace_limit > 0 && (long long)pl.ws_bytes > o.workspace_limit) {
         g_last_err = "workspace of the pattern exceeds the budget";
         return CAPS_ERR_BUDGET;
     }
     if (o.form == CAPS_FORM_SPLIT) CAPS_TRY(status_buffer());
     CAPS_TRY(ensure(g_arena, pl.total));
-    CAPS_TRY(plan(A, B, C, d, pat, o, g_arena.ptr, pl, host_overlap));
+    CAPS_TRY(plan(A, B, C, d, pat, o, g_arena.ptr, pl, host_overlap, extras));
     double pt[3] = {0, 0, 0};
     long long l0 = g_launches;
     KernelTiming kt;

@@ -393,3 +393,25 @@ def test_host_entry_float_bit_identical_to_device(caps, oracle_mod, cuda, form, 
                   "b" * r, form=form)
     torch.cuda.synchronize()
     assert np.array_equal(c, dC.cpu().numpy())
+
+
+@pytest.mark.parametrize("form", ["plain", "split"])
+def test_host_entry_tight_budget_drops_overlap_extras(caps, oracle_mod, cuda, form):
+    """A workspace budget that fits the overlapped host plan only without its
+    extra buffers (the one-pass sums and the early Q5): the call still runs,
+    with the lean passes, and gives the device path's bits."""
+    import torch
+    n, r = 512, 2
+    d = caps.MatDescriptor.make(n, r)
+    q_bytes = (n // 2) ** 2 * 8
+    budget = caps.workspace_size(d, "dd", form=form) + 2 * q_bytes  # Q2's buffers, not ten more quarters
+    rng = np.random.default_rng(77)
+    a = caps_of(oracle_mod, rng.uniform(-1, 1, (n, n)), r)
+    b = caps_of(oracle_mod, rng.uniform(-1, 1, (n, n)), r)
+    c = np.full(n * n, np.nan)
+    caps.multiply(a, b, c, d, "dd", form=form, workspace_limit=budget)
+    assert caps.counters()["workspace_peak_bytes"] <= budget
+    dC = torch.full((n * n,), float("nan"), dtype=torch.float64, device=cuda)
+    caps.multiply(torch.from_numpy(a).to(cuda), torch.from_numpy(b).to(cuda), dC, d, "dd", form=form)
+    torch.cuda.synchronize()
+    assert np.array_equal(c, dC.cpu().numpy())
