@@ -1158,20 +1158,23 @@ __global__ void fill_uniform_kernel(double *p, int64_t n, uint64_t seed, int wid
 }
 
 // Error sums of the tuner's accuracy gate over T instances (C of instance i
-// at c + i * cstride, its reference at r + i * nn): out[0] += sum (c - r)^2,
-// out[1] += sum r^2, out[2] = max |c - r| (infinite where c is not a
-// number), out[3] = max |r|.  out[2], out[3] are non-negative doubles, whose
-// encodings order as the values do.
-__global__ void tune_error_kernel(const double *__restrict__ c, const double *__restrict__ r, int64_t nn, int T,
-                                  int64_t cstride, double *out) {
+// at c + i * cstride, its reference at r + i * nn, (|A||B|) at ab + i *
+// cstride): out[0] += sum (c - r)^2, out[1] += sum r^2, out[2] = max over
+// entries of |c - r| / (|A||B|) (infinite where c is not a number, or where
+// it differs from r on an entry whose |A||B| is 0), out[3] = max |r|.
+// out[2], out[3] are non-negative doubles, whose encodings order as the
+// values do.
+__global__ void tune_error_kernel(const double *__restrict__ c, const double *__restrict__ r,
+                                  const double *__restrict__ ab, int64_t nn, int T, int64_t cstride, double *out) {
     double s2 = 0, r2 = 0, md = 0, mr = 0;
     const int64_t total = nn * T;
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = k / nn, e = k - i * nn;
-        const double y = r[k], d = c[i * cstride + e] - y, ad = fabs(d);
+        const double y = r[k], d = c[i * cstride + e] - y, ad = fabs(d), w = ab[i * cstride + e];
         s2 += d * d;
         r2 += y * y;
-        md = ad == ad ? fmax(md, ad) : INFINITY;
+        const double rel = w > 0.0 ? ad / w : (ad > 0.0 ? INFINITY : 0.0);
+        md = rel == rel ? fmax(md, rel) : INFINITY;
         mr = fmax(mr, fabs(y));
     }
     for (int o = 16; o; o >>= 1) {
@@ -1185,6 +1188,15 @@ __global__ void tune_error_kernel(const double *__restrict__ c, const double *__
         atomicAdd(out + 1, r2);
         atomicMax(reinterpret_cast<unsigned long long *>(out + 2), (unsigned long long)__double_as_longlong(md));
         atomicMax(reinterpret_cast<unsigned long long *>(out + 3), (unsigned long long)__double_as_longlong(mr));
+    }
+}
+
+// |x| of the A and B parts of each instance (3 nn apart, A and B first).
+__global__ void tune_abs_kernel(const double *__restrict__ src, double *__restrict__ dst, int64_t nn, int T) {
+    const int64_t total = 2 * nn * T;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = k / (2 * nn), e = k - i * 2 * nn, x = i * 3 * nn + e;
+        dst[x] = fabs(src[x]);
     }
 }
 
@@ -1207,7 +1219,8 @@ static caps_status run_plan_direct(BatchPlan &p, cudaStream_t s) {
 //      the uniform batch and on a wide-range batch (u 2^k, k in [-20, 20]),
 //      its error against a split reference (depth 0, 55 bits) is no larger
 //      than the plain FP64 form's at the same depth and pattern, both
-//      normwise and in the largest entry.
+//      normwise and in the largest entry relative to |A||B| (the measure the
+//      accuracy target is stated in).
 // The split GEMMs' tiles (residues 128 x 256, digits 128 x 64) are fixed:
 // the operand slicers write their planes in those tiles' layout.  The
 // choices are kept per process and in an on-disk cache (tune_cache_*).
@@ -1218,7 +1231,7 @@ static caps_status run_plan_direct(BatchPlan &p, cudaStream_t s) {
 // (empty: no disk cache), else $HOME/.cache/caps_gb300/autotune.tsv.  A new
 // tuning version (a change of the kernels or axes the choices were made
 // with) leaves older lines unused; deleting the file forces new timings.
-static const char *kTuneVersion = "caps-tune-3";
+static const char *kTuneVersion = "caps-tune-4";
 
 static std::string tune_cache_path() {
     const char *e = getenv("CAPS_AUTOTUNE_CACHE");
@@ -1303,14 +1316,15 @@ struct Tuning {
     int64_t nn = 0;
     double *data = nullptr;  // instance i: A, B, C at data + 3 nn i (+ nn, + 2 nn)
     double *ref = nullptr;   // the gate's reference products, nn per instance
+    double *absd = nullptr;  // |A|, |B| and their product |A||B|, laid out as data
     double *err = nullptr;   // tune_error_kernel's four sums
-    std::vector<BatchItem> items;
+    std::vector<BatchItem> items, abs_items;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
 
     ~Tuning() {
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
-        for (double *p : {data, ref, err})
+        for (double *p : {data, ref, absd, err})
             if (p) cudaFree(p);
     }
 
@@ -1320,9 +1334,9 @@ struct Tuning {
 
     // Plans and runs one candidate: with `ms`, three runs and the best of the
     // last two; without, one run (its products are what the gate reads).
-    caps_status run(const ClassCfg &c, const caps_options &o, double *ms) {
+    caps_status run(const ClassCfg &c, const caps_options &o, double *ms, const std::vector<BatchItem> *its = nullptr) {
         BatchPlan p;
-        p.items = items;
+        p.items = its ? *its : items;
         caps_status st = plan_batch(p, {c}, o);
         double t = 1e30;
         for (int rep = 0; rep < (ms ? 3 : 1) && st == CAPS_OK; rep++) {
@@ -1339,12 +1353,13 @@ struct Tuning {
         return st;
     }
 
-    // Squared error sum and largest entry error of the batch's products
-    // against `ref`.
+    // Squared error sum, and the largest entry error relative to |A||B| (the
+    // measure the split form's accuracy target is stated in), of the batch's
+    // products against `ref`.
     caps_status errors(double &s2, double &maxerr) {
         double h[4] = {0, 0, 0, 0};
         CAPS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof h, 0));
-        tune_error_kernel<<<152 * 4, 256>>>(data + 2 * nn, ref, nn, T, 3 * nn, err);
+        tune_error_kernel<<<152 * 4, 256>>>(data + 2 * nn, ref, absd + 2 * nn, nn, T, 3 * nn, err);
         CAPS_CUDA_TRY(cudaGetLastError());
         CAPS_CUDA_TRY(cudaMemcpy(h, err, sizeof h, cudaMemcpyDeviceToHost));
         s2 = h[0];
@@ -1356,6 +1371,13 @@ struct Tuning {
     caps_status gate(const ClassCfg &base, int bits, const caps_options &o, bool &ok) {
         if (!ref) CAPS_TRY(dev_malloc((void **)&ref, (size_t)nn * T * sizeof(double)));
         if (!err) CAPS_TRY(dev_malloc((void **)&err, 4 * sizeof(double)));
+        if (!absd) {
+            CAPS_TRY(dev_malloc((void **)&absd, (size_t)3 * nn * T * sizeof(double)));
+            for (int i = 0; i < T; i++) {
+                double *d = absd + 3 * nn * i;
+                abs_items.push_back({n, d, d + nn, d + 2 * nn});
+            }
+        }
         caps_options oref = o, oplain = o;
         oref.form = CAPS_FORM_SPLIT;
         oref.slices = oref.diagonals = 0;
@@ -1370,9 +1392,14 @@ struct Tuning {
         cand.bits = bits;
         ok = true;
         caps_status st = CAPS_OK;
+        ClassCfg cabs{n, 0, {0}, 0, DMMA_TILE_64x64, 0};
         for (int wide = 0; wide < 2 && ok && st == CAPS_OK; wide++) {
             fill(wide);
-            st = run(cref, oref, nullptr);
+            // |A||B| of every instance, the scale of each entry's error
+            tune_abs_kernel<<<1024, 256>>>(data, absd, nn, T);
+            if (cudaGetLastError() != cudaSuccess) st = CAPS_ERR_CUDA;
+            if (st == CAPS_OK) st = run(cabs, oplain, nullptr, &abs_items);
+            if (st == CAPS_OK) st = run(cref, oref, nullptr);
             for (int i = 0; i < T && st == CAPS_OK; i++)
                 if (cudaMemcpyAsync(ref + nn * i, data + 3 * nn * i + 2 * nn, (size_t)nn * sizeof(double),
                                     cudaMemcpyDeviceToDevice, 0) != cudaSuccess)

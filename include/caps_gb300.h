@@ -87,7 +87,8 @@ typedef struct caps_options {
  * size -- the fewest (fewest moduli: 17 / 16 / 15) that run faster than 55
  * and whose leaf product, on synthetic uniform and wide-range (u 2^k,
  * |k| <= 20) leaves, is no less accurate than the FP64 DMMA leaf's (squared
- * error sum and largest entry error against a 55-bit reference).  Timed and
+ * error sum, and largest entry error relative to |A||B|, against a 55-bit
+ * reference).  Timed and
  * checked on the device once per leaf size and device, and kept with the
  * autotuner's choices (caps_autotune_info, leaf_gate = 1); make the first
  * such call for a leaf size outside any stream capture. */
@@ -290,7 +291,8 @@ typedef struct {
  *   3. split form where the residues won: operand bits 55 / 52 / 48 (17 / 16 /
  *      15 moduli at K <= 2048), a smaller cap kept only if it is faster and
  *      its error against a split reference is no larger than the plain FP64
- *      form's at the same depth and pattern (normwise and largest entry), on
+ *      form's at the same depth and pattern (normwise, and largest entry
+ *      relative to |A||B|), on
  *      uniform and on wide-range (u 2^k, |k| <= 20) synthetic inputs.
  * No reference counterpart. */
 caps_status caps_autotune_info(int index, caps_tune_info *out);
