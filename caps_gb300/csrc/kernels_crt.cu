@@ -53,6 +53,11 @@ constexpr int RGEMM_THREADS = 448;                // producer, MMA, 8 drain, 4 r
 constexpr unsigned RSTATUS = 0x100;               // status bits of this kernel: RSTATUS << code
 
 struct CrtTables {
+    // the slicer's constants, each in both lanes of a float2 for the packed
+    // fp32 pair instructions: -p_l, 1/p_l, c and cy below
+    float2 np2[LMAX], invp2[LMAX];
+    float2 c2[LMAX][3];
+    float2 cy2[LMAX][LMAX][4];
     float p[LMAX], invp[LMAX];
     float c[LMAX][3];              // balanced 2^(14k) mod p_l, k = 1..3
     float cy[LMAX][LMAX][4];       // [L-1][l][k]: balanced 2^(14k) y_l mod p_l, k = 0..3,
@@ -84,7 +89,10 @@ void build_tables(CrtTables &t) {
             v = (v * 16384) % p;
             long long b = v > p / 2 ? v - p : v;
             t.c[l][k - 1] = (float)b;
+            t.c2[l][k - 1] = make_float2((float)b, (float)b);
         }
+        t.np2[l] = make_float2(-(float)p, -(float)p);
+        t.invp2[l] = make_float2(t.invp[l], t.invp[l]);
     }
     t.lg[0] = 0;
     for (int L = 1; L <= LMAX; L++) {
@@ -97,7 +105,11 @@ void build_tables(CrtTables &t) {
         t.m_inv[L - 1] = (float)(1.0 / (double)M);
         for (int l = 0; l < LMAX; l++) {
             if (l >= L) {
-                for (int k = 0; k < 4; k++) t.Ml[L - 1][l][k] = t.cy[L - 1][l][k] = 0;
+                for (int k = 0; k < 4; k++) {
+                    t.Ml[L - 1][l][k] = 0;
+                    t.cy[L - 1][l][k] = 0;
+                    t.cy2[L - 1][l][k] = make_float2(0.f, 0.f);
+                }
                 continue;
             }
             const u128 Ml = M / (u128)MODULI[l];
@@ -105,6 +117,7 @@ void build_tables(CrtTables &t) {
             long long v = y;
             for (int k = 0; k < 4; k++) {
                 t.cy[L - 1][l][k] = (float)(v > p / 2 ? v - p : v);
+                t.cy2[L - 1][l][k] = make_float2(t.cy[L - 1][l][k], t.cy[L - 1][l][k]);
                 v = (v * 16384) % p;
             }
             for (int k = 0; k < 4; k++) t.Ml[L - 1][l][k] = (uint32_t)(Ml >> (32 * k));
@@ -187,23 +200,44 @@ __device__ __forceinline__ Limbs scaled_limbs14(double x, int f) {
     return l;
 }
 
-// the balanced residue of x's integer modulo p_l, as an fp32 value (|r| <= 90)
-__device__ __forceinline__ float residue_f32(const Limbs &x, int l) {
-    const float y = fmaf(x.a[3], c_crt.c[l][2], fmaf(x.a[2], c_crt.c[l][1], fmaf(x.a[1], c_crt.c[l][0], x.a[0])));
-    const float q = fmaf(y, c_crt.invp[l], MAGIC) - MAGIC;
-    return fmaf(-q, c_crt.p[l], y);
+// The balanced residues (|r| <= 90) of two values' integers modulo p_l, one
+// per lane, on packed fp32 pair instructions: each lane performs exactly
+// the scalar sequence y = a0 + a1 c0 + a2 c1 + a3 c2 (three fused
+// multiply-adds, innermost first), q = fl(y fl(1/p) + MAGIC) - MAGIC,
+// r = fl(y - q p), with round-to-nearest per lane as the scalar forms, at
+// half the issued instructions.
+struct Limbs2 {
+    float2 a[4];  // lane x: the first value's limbs, lane y: the second's
+};
+
+__device__ __forceinline__ Limbs2 pair_limbs(const Limbs &u, const Limbs &v) {
+    Limbs2 x;
+#pragma unroll
+    for (int k = 0; k < 4; k++) x.a[k] = make_float2(u.a[k], v.a[k]);
+    return x;
 }
 
-// the same for x's integer times y_l (the CRT coefficient of modulus l among
+__device__ __forceinline__ float2 reduce_pair(float2 y, int l) {
+    const float2 q = __fadd2_rn(__ffma2_rn(y, c_crt.invp2[l], make_float2(MAGIC, MAGIC)),
+                                make_float2(-MAGIC, -MAGIC));
+    return __ffma2_rn(q, c_crt.np2[l], y);
+}
+
+__device__ __forceinline__ float2 residue_pair(const Limbs2 &x, int l) {
+    const float2 *c = c_crt.c2[l];
+    return reduce_pair(__ffma2_rn(x.a[3], c[2], __ffma2_rn(x.a[2], c[1], __ffma2_rn(x.a[1], c[0], x.a[0]))), l);
+}
+
+// the same for the integers times y_l (the CRT coefficient of modulus l among
 // L): A's residues carry y_l, so each modulus's product sum is already
 // y_l A'B' mod p_l, the term the CRT needs.  |y| <= 4 * 8192 * 90 < 2^21.5,
 // so y / p is within 2^-9.3 of y * fl(1/p), still inside the half-integer
 // margin of 2^-8.5.
-__device__ __forceinline__ float residue_y_f32(const Limbs &x, int L, int l) {
-    const float *cy = c_crt.cy[L - 1][l];
-    const float y = fmaf(x.a[3], cy[3], fmaf(x.a[2], cy[2], fmaf(x.a[1], cy[1], x.a[0] * cy[0])));
-    const float q = fmaf(y, c_crt.invp[l], MAGIC) - MAGIC;
-    return fmaf(-q, c_crt.p[l], y);
+__device__ __forceinline__ float2 residue_y_pair(const Limbs2 &x, int L, int l) {
+    const float2 *cy = c_crt.cy2[L - 1][l];
+    return reduce_pair(
+        __ffma2_rn(x.a[3], cy[3], __ffma2_rn(x.a[2], cy[2], __ffma2_rn(x.a[1], cy[1], __fmul2_rn(x.a[0], cy[0])))),
+        l);
 }
 
 // two residues as packed bf16: |r| <= 90 has at most 7 significant bits, so
@@ -263,18 +297,20 @@ __global__ void crt_resolve_kernel(char *__restrict__ ws, Geo g, SplitParams p) 
 }
 
 // ---------------------------------------------------------------- slice
-// The residues of 8 values modulo each of the first NL moduli (A side:
-// premultiplied by the CRT coefficients of NL moduli), 8 bf16 per plane.
+// The residues of 4 pairs of values modulo each of the first NL moduli (A
+// side: premultiplied by the CRT coefficients of NL moduli), 8 bf16 per plane.
 template <int NL>
-__device__ __forceinline__ void write_residues_unrolled(const Limbs (&x)[8], char *dst, size_t plane_stride,
+__device__ __forceinline__ void write_residues_unrolled(const Limbs2 (&x)[4], char *dst, size_t plane_stride,
                                                         int side) {
     if (side == 0) {
 #pragma unroll
         for (int l = 0; l < NL; l++) {
             uint32_t w[4];
 #pragma unroll
-            for (int q = 0; q < 4; q++)
-                w[q] = pack_bf16x2(residue_y_f32(x[2 * q], NL, l), residue_y_f32(x[2 * q + 1], NL, l));
+            for (int q = 0; q < 4; q++) {
+                const float2 r = residue_y_pair(x[q], NL, l);
+                w[q] = pack_bf16x2(r.x, r.y);
+            }
             *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
         }
     } else {
@@ -282,7 +318,10 @@ __device__ __forceinline__ void write_residues_unrolled(const Limbs (&x)[8], cha
         for (int l = 0; l < NL; l++) {
             uint32_t w[4];
 #pragma unroll
-            for (int q = 0; q < 4; q++) w[q] = pack_bf16x2(residue_f32(x[2 * q], l), residue_f32(x[2 * q + 1], l));
+            for (int q = 0; q < 4; q++) {
+                const float2 r = residue_pair(x[q], l);
+                w[q] = pack_bf16x2(r.x, r.y);
+            }
             *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
         }
     }
@@ -343,35 +382,26 @@ __device__ __forceinline__ void crt_slice_tile(const LeafTask *__restrict__ task
     double v[8];
 #pragma unroll
     for (int e = 0; e < 8; e++) v[e] = (live && k0 + e < M) ? __ldg(src + e * sk) : 0.0;
-    Limbs x[8];
+    Limbs2 x[4];
 #pragma unroll
-    for (int e = 0; e < 8; e++) x[e] = scaled_limbs14(v[e], f);
+    for (int q = 0; q < 4; q++) x[q] = pair_limbs(scaled_limbs14(v[2 * q], f), scaled_limbs14(v[2 * q + 1], f));
     switch (L) {
         // float data need 17 moduli at 55 bits, 16 or 15 under an operand-bit
-        // cap: unrolled, the FMAs take their constants straight from the
-        // constant bank, with no per-modulus loads or loop bookkeeping
+        // cap: unrolled, the constants' addresses are fixed, with no
+        // per-modulus address arithmetic or loop bookkeeping
         case 17: write_residues_unrolled<17>(x, dst, plane_stride, side); break;
         case 16: write_residues_unrolled<16>(x, dst, plane_stride, side); break;
         case 15: write_residues_unrolled<15>(x, dst, plane_stride, side); break;
         default:
-            if (side == 0) {
 #pragma unroll 1
-                for (int l = 0; l < L; l++) {
-                    uint32_t w[4];
+            for (int l = 0; l < L; l++) {
+                uint32_t w[4];
 #pragma unroll
-                    for (int q = 0; q < 4; q++)
-                        w[q] = pack_bf16x2(residue_y_f32(x[2 * q], L, l), residue_y_f32(x[2 * q + 1], L, l));
-                    *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
+                for (int q = 0; q < 4; q++) {
+                    const float2 r = side == 0 ? residue_y_pair(x[q], L, l) : residue_pair(x[q], l);
+                    w[q] = pack_bf16x2(r.x, r.y);
                 }
-            } else {
-#pragma unroll 1
-                for (int l = 0; l < L; l++) {
-                    uint32_t w[4];
-#pragma unroll
-                    for (int q = 0; q < 4; q++)
-                        w[q] = pack_bf16x2(residue_f32(x[2 * q], l), residue_f32(x[2 * q + 1], l));
-                    *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
-                }
+                *reinterpret_cast<uint4 *>(dst + (size_t)l * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
             }
     }
 }
