@@ -44,7 +44,7 @@ C_ABI_SYMBOLS = [
     "caps_status_string", "caps_last_cuda_error", "caps_debug_fail_allocations", "caps_release_cache",
     "caps_leaf_gemm_split_noalloc_dev", "caps_autotune_entry", "caps_chol_mult_dev", "caps_chol_mult_host",
     "caps_debug_starve_split_gemm", "caps_autotune_entry_ex", "caps_autotune_info",
-    "caps_rect_mm_dev", "caps_rect_mm_host",
+    "caps_rect_mm_dev", "caps_rect_mm_host", "caps_debug_tune_cache_line",
 ]
 
 
@@ -161,6 +161,9 @@ def lib() -> ctypes.CDLL:
         L.caps_rect_mm_host.restype = ctypes.c_int
         L.caps_autotune_info.argtypes = [ctypes.c_int, ctypes.POINTER(TuneInfo)]
         L.caps_autotune_info.restype = ctypes.c_int
+        L.caps_debug_tune_cache_line.argtypes = [ctypes.c_char_p, ctypes.c_char_p, i_, i_, i_, i_,
+                                                 ctypes.POINTER(TuneInfo)]
+        L.caps_debug_tune_cache_line.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -341,18 +344,38 @@ def autotune_table() -> list:
     the entry came from the on-disk cache, and seconds per instance."""
     out = []
     i = 0
-    names = {0: None, 1: "digits", 2: "residues"}
     while True:
         t = TuneInfo()
         if lib().caps_autotune_info(i, ctypes.byref(t)):
             return out
-        out.append({"n": t.n, "form": "split" if t.form == 1 else "plain", "nrec": t.nrec,
-                    "pattern": t.pattern.decode(), "scheme": names.get(t.scheme, t.scheme),
-                    "tile": [t.tile_rows, t.tile_cols], "operand_bits": t.operand_bits, "moduli": t.moduli,
-                    "gate_rejected": t.gate_rejected, "leaf_gate": bool(t.leaf_gate),
-                    "from_cache": bool(t.from_cache),
-                    "seconds_per_instance": t.seconds})
+        out.append(_tune_dict(t))
         i += 1
+
+
+def _tune_dict(t: TuneInfo) -> dict:
+    names = {0: None, 1: "digits", 2: "residues"}
+    return {"n": t.n, "form": "split" if t.form == 1 else "plain", "nrec": t.nrec,
+            "pattern": t.pattern.decode(), "scheme": names.get(t.scheme, t.scheme),
+            "tile": [t.tile_rows, t.tile_cols], "operand_bits": t.operand_bits, "moduli": t.moduli,
+            "gate_rejected": t.gate_rejected, "leaf_gate": bool(t.leaf_gate),
+            "from_cache": bool(t.from_cache),
+            "seconds_per_instance": t.seconds}
+
+
+def debug_tune_cache_line(line: str, device_key: str, n: int, form: int | str = CAPS_FORM_SPLIT,
+                          slices: int = 0, scheme: int | str = 0):
+    """caps_debug_tune_cache_line: the choice one line of the autotuner's
+    on-disk cache gives for size n under (form, slices, scheme) on the device
+    keyed `device_key`, as an autotune_table() entry, or None when the line
+    does not apply or is damaged.  Host only: no device call."""
+    if isinstance(form, str):
+        form = {"plain": CAPS_FORM_PLAIN, "split": CAPS_FORM_SPLIT}[form]
+    if isinstance(scheme, str):
+        scheme = SPLIT_SCHEMES[scheme]
+    t = TuneInfo()
+    ok = lib().caps_debug_tune_cache_line(line.encode(), device_key.encode(), int(n), int(form), int(slices),
+                                          int(scheme), ctypes.byref(t))
+    return _tune_dict(t) if ok else None
 
 
 def workspace_size(desc: MatDescriptor, pattern=None, form: int | str = CAPS_FORM_PLAIN,

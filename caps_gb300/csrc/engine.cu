@@ -1254,26 +1254,46 @@ static std::string tune_device_key() {
     return name + "/" + std::to_string(prop.multiProcessorCount);
 }
 
+// One line of the on-disk cache (tune_cache_store's format): true if it
+// holds a usable choice for size n under options o on device `dev`.  Each
+// line is parsed on its own, so a short or damaged line costs only itself.
+static bool parse_tune_line(const char *line, const std::string &dev, int n, const caps_options &o,
+                            TuneEntry &out) {
+    char ver[64], dk[256], pat[16];
+    int fn, fform, fslices, fscheme, nrec, chosen, tile, bits, rejected;
+    double sec;
+    if (sscanf(line, "%63s %255s %d %d %d %d %d %15s %d %d %d %d %lf", ver, dk, &fn, &fform, &fslices, &fscheme,
+               &nrec, pat, &chosen, &tile, &bits, &rejected, &sec) != 13)
+        return false;
+    if (strcmp(ver, kTuneVersion) || dev != dk || fn != n || fform != o.form || fslices != o.slices ||
+        fscheme != o.split_scheme || nrec < 0 || nrec > 3 || tile < 0 || tile >= DMMA_TILES || bits < 0 ||
+        bits > 55 || chosen < CAPS_SPLIT_AUTO || chosen > CAPS_SPLIT_RESIDUES)
+        return false;
+    // the tuner writes nrec steps of 'b' or 'd' ("-" for none); anything
+    // else is a damaged or foreign line
+    const size_t plen = strcmp(pat, "-") ? strlen(pat) : 0;
+    bool pat_ok = plen == (size_t)nrec;
+    for (size_t i = 0; i < plen && pat_ok; i++) pat_ok = pat[i] == 'b' || pat[i] == 'd';
+    if (!pat_ok) return false;
+    TuneEntry t{n, o.form, o.slices, nrec, {0}, sec, o.split_scheme, chosen, 1, tile, bits, rejected};
+    memcpy(t.pat, pat, plen);
+    out = t;
+    return true;
+}
+
 static bool tune_cache_lookup(int n, const caps_options &o, TuneEntry &out) {
     const std::string path = tune_cache_path(), dev = tune_device_key();
     if (path.empty() || dev.empty()) return false;
     FILE *f = fopen(path.c_str(), "r");
     if (!f) return false;
-    char ver[64], dk[256], pat[16];
-    int fn, fform, fslices, fscheme, nrec, chosen, tile, bits, rejected;
-    double sec;
+    char line[1024];
     bool found = false;
-    while (fscanf(f, "%63s %255s %d %d %d %d %d %15s %d %d %d %d %lf", ver, dk, &fn, &fform, &fslices, &fscheme,
-                  &nrec, pat, &chosen, &tile, &bits, &rejected, &sec) == 13) {
-        if (strcmp(ver, kTuneVersion) || dev != dk || fn != n || fform != o.form || fslices != o.slices ||
-            fscheme != o.split_scheme || nrec < 0 || nrec > 3 || tile < 0 || tile >= DMMA_TILES || bits < 0 ||
-            bits > 55)
-            continue;
-        TuneEntry t{n, o.form, o.slices, nrec, {0}, sec, o.split_scheme, chosen, 1, tile, bits, rejected};
-        if (strcmp(pat, "-")) memcpy(t.pat, pat, std::min<size_t>(strlen(pat), 7));
-        out = t;
-        found = true;  // the last matching line wins
-    }
+    TuneEntry t;
+    while (fgets(line, sizeof line, f))
+        if (parse_tune_line(line, dev, n, o, t)) {
+            out = t;
+            found = true;  // the last matching line wins
+        }
     fclose(f);
     return found;
 }
@@ -2067,10 +2087,7 @@ caps_status caps_autotune_entry_ex(int index, int *n, int *form, int *nrec, char
     return CAPS_OK;
 }
 
-caps_status caps_autotune_info(int index, caps_tune_info *out) {
-    std::lock_guard<std::recursive_mutex> g(g_mu);
-    if (!out || index < 0 || index >= (int)g_tune.size()) return CAPS_ERR_ARG;
-    const TuneEntry &t = g_tune[index];
+static void tune_info_from_entry(const TuneEntry &t, caps_tune_info *out) {
     memset(out, 0, sizeof *out);
     out->n = t.n;
     out->form = t.form;
@@ -2094,7 +2111,26 @@ caps_status caps_autotune_info(int index, caps_tune_info *out) {
     }
     out->from_cache = t.from_cache;
     out->seconds = t.seconds;
+}
+
+caps_status caps_autotune_info(int index, caps_tune_info *out) {
+    std::lock_guard<std::recursive_mutex> g(g_mu);
+    if (!out || index < 0 || index >= (int)g_tune.size()) return CAPS_ERR_ARG;
+    tune_info_from_entry(g_tune[index], out);
     return CAPS_OK;
+}
+
+int caps_debug_tune_cache_line(const char *line, const char *device_key, int n, int form, int slices,
+                               int split_scheme, caps_tune_info *out) {
+    if (!line || !device_key) return 0;
+    caps_options o{};
+    o.form = form;
+    o.slices = slices;
+    o.split_scheme = split_scheme;
+    TuneEntry t;
+    if (!parse_tune_line(line, device_key, n, o, t)) return 0;
+    if (out) tune_info_from_entry(t, out);
+    return 1;
 }
 
 caps_status caps_rect_mm_dev(const double *A, const double *B, double *C, int m, int n, int k, int r,

@@ -314,6 +314,16 @@ void caps_debug_fail_allocations(int count);
  * hang is involved.  count <= 0 disables. */
 void caps_debug_starve_split_gemm(int count);
 
+/* Test hook for the autotuner's on-disk cache (host only, no device call):
+ * 1 if `line`, one line of the cache file, holds a usable choice for size n
+ * under (form, slices, split_scheme) on the device whose key is
+ * `device_key` (the device name with blanks as '_', '/', its SM count), and
+ * then fills *out (if not NULL) as caps_autotune_info would; 0 for a line
+ * of another version, device or size, or a damaged one (a field missing or
+ * out of range, a pattern that is not nrec steps of 'b' / 'd'). */
+int caps_debug_tune_cache_line(const char *line, const char *device_key, int n, int form, int slices,
+                               int split_scheme, caps_tune_info *out);
+
 /* Releases cached workspace and plans. */
 void caps_release_cache(void);
 

@@ -266,3 +266,50 @@ def test_rect_bench_links_against_library(caps, tmp_path):
     assert r.returncode == 0, r.stdout
     syms = subprocess.run(["nm", out], stdout=subprocess.PIPE, text=True).stdout
     assert " U _Z6rectMMPdS_S_iiiiiPcPi" in syms  # left to the shared library
+
+
+def test_autotune_cache_lines_checked_one_by_one(caps):
+    """The on-disk autotune cache's reader (host only): a line applies only to
+    its own version, device, size and options; a damaged line is skipped on
+    its own, whatever it holds."""
+    dev = "NVIDIA_GB300/152"
+
+    def line(*f):
+        return "\t".join(str(x) for x in f) + "\n"
+
+    # version, device, n, form, slices, scheme asked, nrec, pattern, scheme chosen, tile, bits, rejected, s
+    split1792 = line("caps-tune-4", dev, 1792, 1, 0, 0, 0, "-", 2, 0, 55, 2, 0.0104)
+    t = caps.debug_tune_cache_line(split1792, dev, 1792, "split")
+    assert t == {"n": 1792, "form": "split", "nrec": 0, "pattern": "", "scheme": "residues", "tile": [128, 256],
+                 "operand_bits": 55, "moduli": 17, "gate_rejected": 2, "leaf_gate": False, "from_cache": True,
+                 "seconds_per_instance": 0.0104}
+    t = caps.debug_tune_cache_line(line("caps-tune-4", dev, 3584, 1, 0, 0, 1, "b", 2, 0, 52, 1, 0.7), dev, 3584,
+                                   "split")
+    assert (t["pattern"], t["operand_bits"], t["moduli"]) == ("b", 52, 16)
+    t = caps.debug_tune_cache_line(line("caps-tune-4", dev, 448, 1, 0, 0, 0, "-", 1, 0, 0, 0, 1e-3), dev, 448,
+                                   "split")
+    assert (t["scheme"], t["tile"], t["moduli"]) == ("digits", [128, 64], 0)
+    t = caps.debug_tune_cache_line(line("caps-tune-4", dev, 1792, 0, 0, 0, 2, "bb", 0, 2, 0, 0, 0.4), dev, 1792,
+                                   "plain")
+    assert (t["form"], t["pattern"], t["scheme"], t["tile"]) == ("plain", "bb", None, [128, 64])
+    # a single multiply's leaf-gate choice is kept under the scheme asked for plus 8
+    t = caps.debug_tune_cache_line(line("caps-tune-4", dev, 2048, 1, 0, 10, 0, "-", 2, 0, 55, 2, 0.01), dev, 2048,
+                                   "split", scheme=10)
+    assert t["leaf_gate"] and t["moduli"] == 17
+    # another version, device, size, form or scheme asked: not this choice
+    assert caps.debug_tune_cache_line(split1792.replace("caps-tune-4", "caps-tune-3"), dev, 1792, "split") is None
+    assert caps.debug_tune_cache_line(split1792, "NVIDIA_B200/148", 1792, "split") is None
+    assert caps.debug_tune_cache_line(split1792, dev, 896, "split") is None
+    assert caps.debug_tune_cache_line(split1792, dev, 1792, "plain") is None
+    assert caps.debug_tune_cache_line(split1792, dev, 1792, "split", scheme="residues") is None
+    # damaged lines
+    for bad in [line("caps-tune-4", dev, 1792, 1, 0, 0, 2, "b", 2, 0, 55, 0, 0.1),     # pattern shorter than nrec
+                line("caps-tune-4", dev, 1792, 1, 0, 0, 1, "x", 2, 0, 55, 0, 0.1),     # not a b/d step
+                line("caps-tune-4", dev, 1792, 1, 0, 0, 0, "b", 2, 0, 55, 0, 0.1),     # steps at depth 0
+                line("caps-tune-4", dev, 1792, 1, 0, 0, 4, "bbbb", 2, 0, 55, 0, 0.1),  # deeper than the tuner goes
+                line("caps-tune-4", dev, 1792, 1, 0, 0, 0, "-", 2, 3, 55, 0, 0.1),     # no such tile
+                line("caps-tune-4", dev, 1792, 1, 0, 0, 0, "-", 2, 0, 56, 0, 0.1),     # bits above 55
+                line("caps-tune-4", dev, 1792, 1, 0, 0, 0, "-", 3, 0, 55, 0, 0.1),     # no such scheme
+                line("caps-tune-4", dev, 1792, 1, 0, 0, 0, "-", 2, 0, 55, 0),          # a field missing
+                ""]:
+        assert caps.debug_tune_cache_line(bad, dev, 1792, "split") is None, bad
